@@ -1,0 +1,149 @@
+/*
+ * nbg.h -- C ABI of libnbg_cuda, the GB300 (sm_103a) implementation of
+ * NbodyGradient.jl's AHL21 integration with forward Jacobian propagation and
+ * transit timing.
+ *
+ * Conventions (all entry points):
+ *   - Arrays are Julia column-major Float64 (double) unless noted, exactly as
+ *     the reference State / TransitTiming hold them:
+ *       x, v, xerror, verror : 3 x n           (x[k + 3 i])
+ *       m                    : n
+ *       jac_step, jac_error, jac_init : 7n x 7n (J[r + 7n c]; body i owns rows
+ *                              7i..7i+6 ordered x, y, z, vx, vy, vz, m)
+ *       dqdt                 : 7n
+ *       pair                 : n x n uint8 (Julia Bool), pair[i + n j]
+ *       tt                   : n x ntt
+ *       dtdq0, dtdelements   : n x ntt x 7 x n   (A[j + n(c + ntt(k + 7p))])
+ *       count                : n int64
+ *   - Body indices are 0-based in this ABI (the Julia shim passes ti - 1).
+ *   - Return value: 0 on success, a negative NBG_E* code on failure; the
+ *     message is available from nbg_last_error() on the calling thread.
+ *   - The library never keeps a caller pointer after a call returns.
+ *   - A context owns one CUDA stream and its device buffers; calls on one
+ *     context must not overlap.  Different contexts may be used from
+ *     different threads.
+ */
+#ifndef NBG_H
+#define NBG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NBG_OK 0
+#define NBG_EINVAL (-1)       /* invalid argument                          */
+#define NBG_ECUDA (-2)        /* CUDA runtime error                        */
+#define NBG_ENOMEM (-3)       /* device allocation failed / budget exceeded */
+#define NBG_EUNSUPPORTED (-4) /* outside the built configuration (n range) */
+#define NBG_ENONFINITE (-5)   /* a system produced non-finite values        */
+#define NBG_ETIMEOUT (-6)     /* a bounded wait ran out                     */
+#define NBG_ECANCELLED (-7)   /* request cancelled                          */
+
+#define NBG_MIN_BODIES 2
+#define NBG_MAX_BODIES 10
+
+/* Per-system status bits written by the batched entry points. */
+#define NBG_STATUS_NONFINITE 1u     /* x, v or J not finite at the end          */
+#define NBG_STATUS_NTT_OVERFLOW 2u  /* more transits than ntt (counted, dropped) */
+#define NBG_STATUS_NEWTON_ITMAX 4u  /* a transit Newton search hit ITMAX = 20    */
+
+typedef struct nbg_context nbg_context;
+
+/* Create / destroy a context on CUDA device `device`.
+ * Replaces: nothing in the reference (it is single-threaded Julia); the Julia
+ * shim creates one context per session. */
+int nbg_create(int device, nbg_context** out);
+int nbg_destroy(nbg_context* ctx);
+
+/* Copy the calling thread's last error message into buf (NUL-terminated). */
+int nbg_last_error(char* buf, size_t len);
+
+/* Library version (major * 10000 + minor * 100 + patch). */
+int nbg_version(void);
+
+typedef struct {
+  char name[128];
+  int sm_count;
+  int cc_major, cc_minor;
+  size_t total_mem;
+  int min_bodies, max_bodies;
+} nbg_device_info_t;
+int nbg_device_info(int device, nbg_device_info_t* out);
+
+/*
+ * (intr::Integrator)(s::State{Float64}, tt::TransitTiming{Float64}; grad)
+ * Replaces src/transits/Transits.jl:140-170 (called through :173-180) with
+ * intr.scheme === ahl21!: integrates nsteps = |round(tmax/h)| AHL21 steps from
+ * s.t = *t, detects transits of every body but ti across body ti, refines
+ * them by Newton on partial steps (src/transits/timing.jl:3-109) and, when
+ * grad != 0, propagates jac_step / jac_error / dqdt (ahl21.jl:5-95), fills
+ * dtdq0 and computes dtdelements = dtdq0 * jac_init (timing.jl:112-123).
+ *
+ * In/out exactly as the reference mutates State and TransitTiming: x, v,
+ * xerror, verror, jac_step, jac_error, dqdt, *t (set to t0 + nsteps * h),
+ * tt, dtdq0, dtdelements and count.  Entries of tt / dtdq0 that no transit
+ * of this call writes are left untouched; dtdelements is recomputed for
+ * every transit 1..min(count, ntt) as the reference does.
+ */
+int nbg_integrate_transits(nbg_context* ctx, int n, int ti, double h, double tmax, int grad, double* t,
+                           double* x, double* v, const double* m, double* xerror, double* verror,
+                           double* jac_step, double* jac_error, double* dqdt, const uint8_t* pair,
+                           const double* jac_init, int64_t ntt, double* tt, double* dtdq0, double* dtdelements,
+                           int64_t* count);
+
+/*
+ * Batched form: nsys independent systems integrated in one plan.  Each
+ * system's arrays are laid out exactly as for nbg_integrate_transits and
+ * concatenated system after system in every packed buffer (so the offset of
+ * system s in `x` is sum_{q<s} 3 n_q, in `jac_step` sum_{q<s} (7 n_q)^2, in
+ * `tt` sum_{q<s} n_q ntt_q, in `dtdq0` sum_{q<s} 7 n_q^2 ntt_q, ...).
+ * All pointers are host pointers.  status (may be NULL) receives one
+ * NBG_STATUS_* word per system.  Outputs of every system are treated as
+ * fresh TransitTiming arrays (count must be zero on entry).
+ */
+typedef struct {
+  int32_t n;     /* bodies, NBG_MIN_BODIES..NBG_MAX_BODIES */
+  int32_t ti;    /* 0-based transited body                  */
+  int32_t grad;  /* 0 or 1                                  */
+  int32_t ntt;   /* TransitTiming.ntt                       */
+  double h;      /* Integrator.h                            */
+  double tmax;   /* Integrator.tmax                         */
+} nbg_system_desc;
+
+int nbg_batch_integrate_transits(nbg_context* ctx, int nsys, const nbg_system_desc* desc, double* t, double* x,
+                                 double* v, const double* m, double* xerror, double* verror, double* jac_step,
+                                 double* jac_error, double* dqdt, const uint8_t* pair, const double* jac_init,
+                                 double* tt, double* dtdq0, double* dtdelements, int64_t* count, uint32_t* status);
+
+/*
+ * Same as nbg_batch_integrate_transits, but every array pointer (and desc)
+ * is a DEVICE pointer of the context's device, already resident in HBM.
+ * Used when the caller keeps systems on the GPU between calls.
+ */
+int nbg_batch_integrate_transits_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc_host, double* t,
+                                        double* x, double* v, const double* m, double* xerror, double* verror,
+                                        double* jac_step, double* jac_error, double* dqdt, const uint8_t* pair,
+                                        const double* jac_init, double* tt, double* dtdq0, double* dtdelements,
+                                        int64_t* count, uint32_t* status);
+
+/* Tuning knobs of a context (0 keeps the current value).
+ * chunk_steps: steps per producer/consumer chunk; overlap: run the orbit
+ * producer and the Jacobian consumer on two streams. */
+int nbg_set_tuning(nbg_context* ctx, int chunk_steps, int overlap);
+
+/* Device time (ms) of the last batched call's kernels, measured with CUDA
+ * events on the context's stream: total, orbit-producer share, Jacobian
+ * consumer share. */
+int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double* jacobian_ms);
+
+/* Number of kernels launched by the last call. */
+int64_t nbg_last_launch_count(nbg_context* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NBG_H */

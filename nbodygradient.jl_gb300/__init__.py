@@ -1,0 +1,259 @@
+"""nbodygradient.jl_gb300 -- GB300 (sm_103a) implementation of NbodyGradient.jl's
+AHL21 integration with forward Jacobian propagation and transit timing.
+
+The Python API mirrors the reference's Julia API for this path so that the
+same call sequence works (names, argument meaning and error behaviour):
+
+    ic  = ElementsIC(t0, H, elements)          # src/ics/InitialConditions.jl:142
+    s   = State(ic)                            # src/integrator/Integrator.jl:82
+    tt  = TransitTiming(tmax, ic)              # src/transits/Transits.jl:42
+    intr = Integrator(ahl21, h, t0, tmax)      # src/integrator/Integrator.jl:17
+    intr(s, tt, grad=True)                     # src/transits/Transits.jl:173
+
+fills tt.tt, tt.dtdq0, tt.dtdelements and advances s, computed by libnbg_cuda
+(CUDA, FP64) through its C ABI (include/nbg.h).  Body indices in this Python
+mirror are 1-based where the Julia API is (TransitTiming's ti), 0-based in
+the arrays.  There is no CPU fallback: without the CUDA library or a GPU the
+calls raise NbgError.
+"""
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import Context, NbgError, SystemDesc, default_context, device_info
+from .ics import CartesianIC, Elements, ElementsIC, hierarchy_nested, init_nbody, kepler_init
+
+__all__ = ["Elements", "ElementsIC", "CartesianIC", "State", "TransitTiming", "Integrator", "ahl21", "set_state",
+           "Context", "NbgError", "default_context", "device_info", "integrate_transits_batch", "Batch",
+           "hierarchy_nested", "init_nbody", "kepler_init"]
+
+
+def ahl21(*args, **kwargs):
+    """Scheme marker for Integrator(ahl21, ...); the step itself runs on the GPU."""
+    raise TypeError("ahl21 is the integration scheme passed to Integrator; call the Integrator instead")
+
+
+class State:
+    """Current state of a system (src/integrator/Integrator.jl:49-103)."""
+
+    def __init__(self, ic):
+        x, v, jac_init = ic.init_nbody()
+        n = ic.nbody
+        M = 7 * n
+        self.n = n
+        self.x = np.asfortranarray(x, dtype=np.float64)
+        self.v = np.asfortranarray(v, dtype=np.float64)
+        self.t = np.array([ic.t0], dtype=np.float64)
+        self.m = np.array(ic.m, dtype=np.float64)
+        self.jac_step = np.asfortranarray(np.eye(M))
+        self.dqdt = np.zeros(M)
+        self.jac_init = np.asfortranarray(jac_init, dtype=np.float64)
+        self.pair = np.asfortranarray(np.zeros((n, n), dtype=np.uint8))
+        self.xerror = np.zeros((3, n), order="F")
+        self.verror = np.zeros((3, n), order="F")
+        self.dqdt_error = np.zeros(M)
+        self.jac_error = np.zeros((M, M), order="F")
+
+    def copy(self):
+        o = State.__new__(State)
+        for k, val in self.__dict__.items():
+            o.__dict__[k] = val.copy(order="K") if isinstance(val, np.ndarray) else val
+        return o
+
+    def isfinite(self):
+        return bool(np.all(np.isfinite(self.x)) and np.all(np.isfinite(self.v)) and np.all(np.isfinite(self.jac_step)))
+
+
+def set_state(s_old, s_new):
+    """set_state! (src/integrator/Integrator.jl:123-134)."""
+    for k in ("t", "x", "v", "jac_step", "xerror", "verror", "jac_error", "dqdt", "dqdt_error"):
+        getattr(s_old, k)[...] = getattr(s_new, k)
+
+
+def _ntt(tmax, periods):
+    periods = np.asarray(periods, dtype=np.float64)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        q = tmax / periods
+    ok = np.isfinite(q)
+    return int(np.max(np.ceil(np.abs(q[ok])).astype(np.int64) + 3))
+
+
+class TransitTiming:
+    """Transit times and derivatives (src/transits/Transits.jl:14-56).  ti is 1-based."""
+
+    def __init__(self, tmax, ic, ti=1):
+        n = ic.nbody
+        if not (1 <= ti <= n):
+            raise ValueError("ti must be in 1..%d" % n)
+        ntt = _ntt(tmax, ic.elements[:, 1])
+        self.n, self.ntt, self.ti = n, ntt, ti
+        self.tt = np.zeros((n, ntt), order="F")
+        self.dtdq0 = np.zeros((n, ntt, 7, n), order="F")
+        self.dtdelements = np.zeros((n, ntt, 7, n), order="F")
+        self.count = np.zeros(n, dtype=np.int64)
+        self.occs = [i for i in range(1, n + 1) if i != ti]
+
+    def zero_out(self):
+        for a in (self.tt, self.dtdq0, self.dtdelements):
+            a[...] = 0.0
+        self.count[...] = 0
+
+
+class Integrator:
+    """Integrator(scheme, h, t0, tmax) (src/integrator/Integrator.jl:17-31).
+
+    Accepted forms, as in the reference: Integrator(ahl21, h, t0, tmax),
+    Integrator(ahl21, h, tmax), Integrator(h, tmax).
+    """
+
+    def __init__(self, *args):
+        if args and callable(args[0]):
+            scheme, rest = args[0], args[1:]
+        else:
+            scheme, rest = ahl21, args
+        if scheme is not ahl21:
+            raise NbgError(_lib.NBG_EUNSUPPORTED, "only the ahl21 scheme is implemented on the GPU")
+        if len(rest) == 3:
+            h, t0, tmax = rest
+        elif len(rest) == 2:
+            h, tmax = rest
+            t0 = 0.0
+        else:
+            raise TypeError("Integrator(scheme, h, t0, tmax) or Integrator(scheme, h, tmax)")
+        self.scheme = scheme
+        self.h, self.t0, self.tmax = float(h), float(t0), float(tmax)
+
+    def __call__(self, s, tt=None, grad=True, ctx=None):
+        if tt is None or not isinstance(tt, TransitTiming):
+            raise NbgError(_lib.NBG_EUNSUPPORTED,
+                           "this build implements intr(s, tt::TransitTiming; grad) on the GPU")
+        ctx = ctx or default_context()
+        L = _lib.load()
+        p = _lib.ptr
+        _lib.check(L.nbg_integrate_transits(
+            ctx.handle, s.n, tt.ti - 1, self.h, self.tmax, int(bool(grad)), p(s.t), p(s.x), p(s.v), p(s.m),
+            p(s.xerror), p(s.verror), p(s.jac_step), p(s.jac_error), p(s.dqdt), p(s.pair, _lib._U8), p(s.jac_init),
+            tt.ntt, p(tt.tt), p(tt.dtdq0), p(tt.dtdelements), p(tt.count, _lib._I64)))
+
+
+class Batch:
+    """Packed arrays of many systems in the C ABI's batched layout.
+
+    Every field is one flat float64 (int64 / uint8) array holding the
+    systems' Julia column-major arrays back to back.  Built from State /
+    TransitTiming pairs or directly from packed arrays; run() integrates all
+    systems in one GPU plan.
+    """
+
+    FIELDS = ("t", "x", "v", "m", "xerror", "verror", "jac_step", "jac_error", "dqdt", "pair", "jac_init", "tt",
+              "dtdq0", "dtdelements", "count")
+
+    def __init__(self, n, ti, h, tmax, ntt, grad=True):
+        n = np.atleast_1d(np.asarray(n, dtype=np.int32))
+        nsys = len(n)
+
+        def bc(a, dt):
+            a = np.asarray(a, dtype=dt)
+            return np.broadcast_to(a, (nsys,)).copy() if a.ndim == 0 else a.astype(dt)
+
+        self.nsys = nsys
+        self.n = n
+        self.ti = bc(ti, np.int32)
+        self.h = bc(h, np.float64)
+        self.tmax = bc(tmax, np.float64)
+        self.ntt = bc(ntt, np.int32)
+        self.grad = bc(int(grad) if np.ndim(grad) == 0 else grad, np.int32)
+        M = 7 * n.astype(np.int64)
+        self.sizes = {
+            "t": np.ones(nsys, np.int64), "x": 3 * n.astype(np.int64), "v": 3 * n.astype(np.int64),
+            "m": n.astype(np.int64), "xerror": 3 * n.astype(np.int64), "verror": 3 * n.astype(np.int64),
+            "jac_step": M * M, "jac_error": M * M, "dqdt": M, "pair": n.astype(np.int64) ** 2, "jac_init": M * M,
+            "tt": n.astype(np.int64) * self.ntt, "dtdq0": n.astype(np.int64) * self.ntt * 7 * n,
+            "dtdelements": n.astype(np.int64) * self.ntt * 7 * n, "count": n.astype(np.int64),
+        }
+        self.offsets = {k: np.concatenate([[0], np.cumsum(v)]) for k, v in self.sizes.items()}
+        dt = {"pair": np.uint8, "count": np.int64}
+        self.arrays = {k: np.zeros(int(self.offsets[k][-1]), dtype=dt.get(k, np.float64)) for k in self.FIELDS}
+        self.status = np.zeros(nsys, dtype=np.uint32)
+
+    def view(self, field, s):
+        a, b = self.offsets[field][s], self.offsets[field][s + 1]
+        return self.arrays[field][a:b]
+
+    def set_system(self, s, state, timing=None):
+        n = int(self.n[s])
+        if state.n != n:
+            raise ValueError("system %d: n mismatch" % s)
+        self.view("t", s)[:] = state.t
+        for k in ("x", "v", "xerror", "verror", "jac_step", "jac_error", "jac_init", "pair"):
+            self.view(k, s)[:] = np.asarray(getattr(state, k)).ravel(order="F")
+        self.view("m", s)[:] = state.m
+        self.view("dqdt", s)[:] = state.dqdt
+        if timing is not None:
+            self.view("tt", s)[:] = timing.tt.ravel(order="F")
+            self.view("dtdq0", s)[:] = timing.dtdq0.ravel(order="F")
+            self.view("dtdelements", s)[:] = timing.dtdelements.ravel(order="F")
+            self.view("count", s)[:] = timing.count
+
+    def get_system(self, s, state, timing=None):
+        n = int(self.n[s])
+        M = 7 * n
+        state.t[:] = self.view("t", s)
+        state.x[...] = self.view("x", s).reshape((3, n), order="F")
+        state.v[...] = self.view("v", s).reshape((3, n), order="F")
+        state.xerror[...] = self.view("xerror", s).reshape((3, n), order="F")
+        state.verror[...] = self.view("verror", s).reshape((3, n), order="F")
+        state.jac_step[...] = self.view("jac_step", s).reshape((M, M), order="F")
+        state.jac_error[...] = self.view("jac_error", s).reshape((M, M), order="F")
+        state.dqdt[...] = self.view("dqdt", s)
+        if timing is not None:
+            ntt = timing.ntt
+            timing.tt[...] = self.view("tt", s).reshape((n, ntt), order="F")
+            timing.dtdq0[...] = self.view("dtdq0", s).reshape((n, ntt, 7, n), order="F")
+            timing.dtdelements[...] = self.view("dtdelements", s).reshape((n, ntt, 7, n), order="F")
+            timing.count[...] = self.view("count", s)
+
+    def descriptors(self):
+        d = (SystemDesc * self.nsys)()
+        for s in range(self.nsys):
+            d[s].n, d[s].ti, d[s].grad, d[s].ntt = int(self.n[s]), int(self.ti[s]), int(self.grad[s]), int(self.ntt[s])
+            d[s].h, d[s].tmax = float(self.h[s]), float(self.tmax[s])
+        return d
+
+    def run(self, ctx=None):
+        """nbg_batch_integrate_transits on the packed host arrays (in place)."""
+        ctx = ctx or default_context()
+        L = _lib.load()
+        p = _lib.ptr
+        a = self.arrays
+        _lib.check(L.nbg_batch_integrate_transits(
+            ctx.handle, self.nsys, self.descriptors(), p(a["t"]), p(a["x"]), p(a["v"]), p(a["m"]), p(a["xerror"]),
+            p(a["verror"]), p(a["jac_step"]), p(a["jac_error"]), p(a["dqdt"]), p(a["pair"], _lib._U8),
+            p(a["jac_init"]), p(a["tt"]), p(a["dtdq0"]), p(a["dtdelements"]), p(a["count"], _lib._I64),
+            p(self.status, _lib._U32)))
+        return self
+
+    def run_device(self, dev_arrays, ctx=None):
+        """nbg_batch_integrate_transits_device on device buffers (a dict of torch CUDA tensors)."""
+        ctx = ctx or default_context()
+        L = _lib.load()
+        d = dev_arrays
+        vp = lambda k: __import__("ctypes").c_void_p(d[k].data_ptr())
+        _lib.check(L.nbg_batch_integrate_transits_device(
+            ctx.handle, self.nsys, self.descriptors(), vp("t"), vp("x"), vp("v"), vp("m"), vp("xerror"),
+            vp("verror"), vp("jac_step"), vp("jac_error"), vp("dqdt"), vp("pair"), vp("jac_init"), vp("tt"),
+            vp("dtdq0"), vp("dtdelements"), vp("count"), __import__("ctypes").c_void_p(self.status.ctypes.data)))
+        return self
+
+
+def integrate_transits_batch(states, timings, h, tmax, grad=True, ctx=None):
+    """Integrate many (State, TransitTiming) pairs in one GPU plan; updates them in place."""
+    nsys = len(states)
+    b = Batch([s.n for s in states], [t.ti - 1 for t in timings], h, tmax, [t.ntt for t in timings], grad)
+    for q in range(nsys):
+        b.set_system(q, states[q], timings[q])
+    b.run(ctx)
+    for q in range(nsys):
+        b.get_system(q, states[q], timings[q])
+    return b.status.copy()

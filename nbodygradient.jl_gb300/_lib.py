@@ -1,0 +1,176 @@
+"""ctypes binding of libnbg_cuda (include/nbg.h).
+
+The library is built in-tree by build.py.  Loading fails loudly when it is
+missing or cannot be loaded: there is no CPU fallback for any entry point.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+NBG_OK = 0
+NBG_EINVAL = -1
+NBG_ECUDA = -2
+NBG_ENOMEM = -3
+NBG_EUNSUPPORTED = -4
+NBG_ENONFINITE = -5
+NBG_ETIMEOUT = -6
+NBG_ECANCELLED = -7
+
+NBG_STATUS_NONFINITE = 1
+NBG_STATUS_NTT_OVERFLOW = 2
+NBG_STATUS_NEWTON_ITMAX = 4
+
+MIN_BODIES = 2
+MAX_BODIES = 10
+
+# Every entry point include/nbg.h declares.
+EXPORTS = (
+    "nbg_create", "nbg_destroy", "nbg_last_error", "nbg_version", "nbg_device_info",
+    "nbg_integrate_transits", "nbg_batch_integrate_transits", "nbg_batch_integrate_transits_device",
+    "nbg_set_tuning", "nbg_last_timing", "nbg_last_launch_count",
+)
+
+
+class NbgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("libnbg_cuda error %d: %s" % (code, msg))
+        self.code = code
+
+
+class SystemDesc(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32), ("ti", ctypes.c_int32), ("grad", ctypes.c_int32), ("ntt", ctypes.c_int32),
+                ("h", ctypes.c_double), ("tmax", ctypes.c_double)]
+
+
+class DeviceInfo(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 128), ("sm_count", ctypes.c_int), ("cc_major", ctypes.c_int),
+                ("cc_minor", ctypes.c_int), ("total_mem", ctypes.c_size_t), ("min_bodies", ctypes.c_int),
+                ("max_bodies", ctypes.c_int)]
+
+
+_D = ctypes.POINTER(ctypes.c_double)
+_U8 = ctypes.POINTER(ctypes.c_uint8)
+_I64 = ctypes.POINTER(ctypes.c_int64)
+_U32 = ctypes.POINTER(ctypes.c_uint32)
+_VP = ctypes.c_void_p
+
+_lib = None
+
+
+def lib_path():
+    return _build.LIB_PATH
+
+
+def load(build_if_missing=True):
+    """Load libnbg_cuda.so (building it first if needed) and declare prototypes."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB_PATH
+    if build_if_missing:
+        path = _build.build()
+    if not os.path.exists(path):
+        raise NbgError(NBG_EUNSUPPORTED, "libnbg_cuda.so not built (run nbodygradient.jl_gb300/build.py)")
+    L = ctypes.CDLL(path)
+    L.nbg_create.argtypes = [ctypes.c_int, ctypes.POINTER(_VP)]
+    L.nbg_destroy.argtypes = [_VP]
+    L.nbg_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    L.nbg_version.argtypes = []
+    L.nbg_device_info.argtypes = [ctypes.c_int, ctypes.POINTER(DeviceInfo)]
+    L.nbg_integrate_transits.argtypes = [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_int, _D, _D, _D, _D, _D, _D, _D, _D, _D, _U8, _D, ctypes.c_int64,
+                                         _D, _D, _D, _I64]
+    batch_args = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc), _D, _D, _D, _D, _D, _D, _D, _D, _D, _U8, _D, _D, _D,
+                  _D, _I64, _U32]
+    L.nbg_batch_integrate_transits.argtypes = batch_args
+    L.nbg_batch_integrate_transits_device.argtypes = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc)] + [_VP] * 16
+    L.nbg_set_tuning.argtypes = [_VP, ctypes.c_int, ctypes.c_int]
+    L.nbg_last_timing.argtypes = [_VP, _D, _D, _D]
+    L.nbg_last_launch_count.argtypes = [_VP]
+    L.nbg_last_launch_count.restype = ctypes.c_int64
+    _lib = L
+    return L
+
+
+def last_error():
+    buf = ctypes.create_string_buffer(512)
+    load().nbg_last_error(buf, 512)
+    return buf.value.decode(errors="replace")
+
+
+def check(rc):
+    if rc != NBG_OK:
+        raise NbgError(rc, last_error())
+    return rc
+
+
+def ptr(a, ctype=_D):
+    if a is None:
+        return ctypes.cast(None, ctype)
+    if not (a.flags["F_CONTIGUOUS"] or a.flags["C_CONTIGUOUS"]):
+        raise ValueError("array must be contiguous")
+    return a.ctypes.data_as(ctype)
+
+
+class Context:
+    """One libnbg_cuda context (a CUDA stream plus cached device buffers)."""
+
+    def __init__(self, device=0):
+        L = load()
+        h = _VP()
+        check(L.nbg_create(device, ctypes.byref(h)))
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h is not None and self._h.value:
+            load().nbg_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_tuning(self, chunk_steps=0, overlap=-1):
+        check(load().nbg_set_tuning(self._h, int(chunk_steps), int(overlap)))
+
+    def last_timing(self):
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(load().nbg_last_timing(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def last_launch_count(self):
+        return int(load().nbg_last_launch_count(self._h))
+
+
+_default_ctx = None
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def device_info(device=0):
+    d = DeviceInfo()
+    check(load().nbg_device_info(device, ctypes.byref(d)))
+    return {"name": d.name.decode(), "sm_count": d.sm_count, "cc": (d.cc_major, d.cc_minor),
+            "total_mem": d.total_mem, "min_bodies": d.min_bodies, "max_bodies": d.max_bodies}
+
+
+def as_f64(a, shape=None):
+    a = np.asfortranarray(a, dtype=np.float64)
+    if shape is not None and a.shape != shape:
+        raise ValueError("expected shape %s, got %s" % (shape, a.shape))
+    return a

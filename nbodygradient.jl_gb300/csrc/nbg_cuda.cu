@@ -1,0 +1,634 @@
+// nbg_cuda.cu -- libnbg_cuda: kernels, orchestration and the C ABI (include/nbg.h).
+//
+// Build: nbodygradient.jl_gb300/build.py compiles this file and nbg_inst.cu
+// once per body count with nvcc -gencode arch=compute_103a,code=sm_103a
+// --fmad=false -O3 and links them into libnbg_cuda.so.  --fmad=false keeps
+// every scalar product and sum separately rounded as in the Julia
+// reference; the kernels use fma() explicitly where a fused product is
+// intended (the BLAS-like operator products).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <tuple>
+#include <string>
+#include <vector>
+
+#include "../../include/nbg.h"
+#include "nbg_layout.cuh"
+
+using namespace nbg;
+
+// ===================================================================== kernels
+
+// Per-system offsets into the caller's packed arrays.
+struct SysOff {
+  long long x, m, J, dqdt, pair, tt, dq, cnt;
+  int n, ntt, grad, pad;
+};
+
+// Gather the caller-layout arrays of one group's systems into its SoA state.
+__global__ void pack_state_kernel(int N, int S, const int* sysidx, const SysOff* off, const double* x,
+                                  const double* v, const double* xe, const double* ve, const double* m,
+                                  const double* dqdt, const long long* count, double* gx, double* gv, double* gxe,
+                                  double* gve, double* gm, double* gdq, long long* gcnt) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S) return;
+  const int gs = sysidx[s];
+  if (gs < 0) return;
+  const SysOff o = off[gs];
+  for (int q = 0; q < 3 * N; q++) {
+    gx[q * S + s] = x[o.x + q];
+    gv[q * S + s] = v[o.x + q];
+    gxe[q * S + s] = xe[o.x + q];
+    gve[q * S + s] = ve[o.x + q];
+  }
+  for (int q = 0; q < N; q++) {
+    gm[q * S + s] = m[o.m + q];
+    gcnt[q * S + s] = count[o.cnt + q];
+  }
+  for (int q = 0; q < 7 * N; q++) gdq[q * S + s] = dqdt[o.dqdt + q];
+}
+
+__global__ void unpack_state_kernel(int N, int S, int grad, const int* sysidx, const SysOff* off, double* x,
+                                    double* v, double* xe, double* ve, double* dqdt, long long* count,
+                                    const double* gx, const double* gv, const double* gxe, const double* gve,
+                                    const double* gdq, const long long* gcnt) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S) return;
+  const int gs = sysidx[s];
+  if (gs < 0) return;
+  const SysOff o = off[gs];
+  for (int q = 0; q < 3 * N; q++) {
+    x[o.x + q] = gx[q * S + s];
+    v[o.x + q] = gv[q * S + s];
+    xe[o.x + q] = gxe[q * S + s];
+    ve[o.x + q] = gve[q * S + s];
+  }
+  for (int q = 0; q < N; q++) count[o.cnt + q] = gcnt[q * S + s];
+  if (grad)
+    for (int q = 0; q < 7 * N; q++) dqdt[o.dqdt + q] = gdq[q * S + s];
+}
+
+// jac_step / jac_error non-mass rows <-> internal [S][6N][7N]; also checks
+// that the mass rows are unit rows with zero error (bad[0] set otherwise).
+__global__ void pack_jac_kernel(int N, int S, const int* sysidx, const SysOff* off, const double* J,
+                                const double* E, double* Jint, double* Eint, int* bad) {
+  const int M = 7 * N, R6 = 6 * N;
+  const long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tot = (long long)S * M * M;
+  if (f >= tot) return;
+  const int s = (int)(f / ((long long)M * M));
+  const int rem = (int)(f % ((long long)M * M));
+  const int c = rem / M, r = rem % M;  // full row r, column c
+  const int gs = sysidx[s];
+  if (gs < 0) return;
+  const long long base = off[gs].J;
+  const double jv = J[base + r + (long long)M * c];
+  const double ev = E[base + r + (long long)M * c];
+  if (r % 7 == 6) {
+    if (jv != ((r == c) ? 1.0 : 0.0) || ev != 0.0) atomicOr(bad, 1);
+    return;
+  }
+  const int rn = (r / 7) * 6 + r % 7;
+  Jint[((size_t)s * R6 + rn) * M + c] = jv;
+  Eint[((size_t)s * R6 + rn) * M + c] = ev;
+  (void)R6;
+}
+
+__global__ void unpack_jac_kernel(int N, int S, const int* sysidx, const SysOff* off, double* J, double* E,
+                                  const double* Jint, const double* Eint) {
+  const int M = 7 * N, R6 = 6 * N;
+  const long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tot = (long long)S * R6 * M;
+  if (f >= tot) return;
+  const int s = (int)(f / ((long long)R6 * M));
+  const int rem = (int)(f % ((long long)R6 * M));
+  const int rn = rem / M, c = rem % M;
+  const int gs = sysidx[s];
+  if (gs < 0) return;
+  const int r = (rn / 6) * 7 + rn % 6;
+  const long long base = off[gs].J;
+  J[base + r + (long long)M * c] = Jint[((size_t)s * R6 + rn) * M + c];
+  E[base + r + (long long)M * c] = Eint[((size_t)s * R6 + rn) * M + c];
+}
+
+// calc_dtdelements! (timing.jl:112-123): one thread per output entry of one
+// system; transits beyond min(count, ntt) are left untouched.
+__global__ void dtdelements_kernel(int nsys, const SysOff* off, const double* dtdq0, const double* jac_init,
+                                   double* dtdel, const long long* count) {
+  const int gs = blockIdx.y + gridDim.y * blockIdx.z;
+  if (gs >= nsys) return;
+  const SysOff o = off[gs];
+  if (!o.grad) return;
+  const int n = o.n, ntt = o.ntt, M = 7 * n;
+  const long long tot = (long long)n * ntt * 7 * n;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(e % n);
+    const long long c = (e / n) % ntt;
+    const int l = (int)((e / ((long long)n * ntt)) % 7);
+    const int k = (int)(e / ((long long)n * ntt * 7));
+    const long long cnt = count[o.cnt + j];
+    if (c >= cnt || c >= ntt) continue;
+    double acc = 0.0;
+    for (int p = 0; p < n; p++)
+      for (int q = 0; q < 7; q++)
+        acc = acc + dtdq0[o.dq + j + (long long)n * (c + (long long)ntt * (q + 7LL * p))] *
+                        jac_init[o.J + (7 * p + q) + (long long)M * (7 * k + l)];
+    dtdel[o.dq + e] = acc;
+  }
+}
+
+// ================================================================ host side
+
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int set_error(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define NBG_CUDA(call)                                                                          \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess) return set_error(NBG_ECUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+struct Buf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct nbg_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::map<std::string, Buf> pool;
+  int chunk_steps = 16;
+  int overlap = 0;
+  double last_total_ms = 0, last_orbit_ms = 0, last_jac_ms = 0;
+  long long last_launches = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  // Grow-only device buffer cache keyed by name.
+  template <class T>
+  int get(const char* name, size_t count, T** out) {
+    size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+    Buf& b = pool[name];
+    if (b.bytes < bytes) {
+      if (b.p) cudaFree(b.p);
+      b.p = nullptr;
+      b.bytes = 0;
+      cudaError_t e = cudaMalloc(&b.p, bytes);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(NBG_ENOMEM, "cudaMalloc(%zu bytes) for %s: %s", bytes, name, cudaGetErrorString(e));
+      }
+      b.bytes = bytes;
+    }
+    *out = (T*)b.p;
+    return NBG_OK;
+  }
+};
+
+namespace {
+
+typedef int (*LaunchFn)(const GroupArgs&, int, cudaStream_t);
+typedef int (*SeedFn)(const GroupArgs&, cudaStream_t);
+const LaunchFn kOrbit[NBG_MAX_BODIES + 1] = {nullptr, nullptr, launch_orbit<2>, launch_orbit<3>, launch_orbit<4>,
+                                             launch_orbit<5>, launch_orbit<6>, launch_orbit<7>, launch_orbit<8>,
+                                             launch_orbit<9>, launch_orbit<10>};
+const LaunchFn kJac[NBG_MAX_BODIES + 1] = {nullptr, nullptr, launch_jac<2>, launch_jac<3>, launch_jac<4>,
+                                           launch_jac<5>, launch_jac<6>, launch_jac<7>, launch_jac<8>,
+                                           launch_jac<9>, launch_jac<10>};
+const SeedFn kSeed[NBG_MAX_BODIES + 1] = {nullptr, nullptr, launch_seed<2>, launch_seed<3>, launch_seed<4>,
+                                          launch_seed<5>, launch_seed<6>, launch_seed<7>, launch_seed<8>,
+                                          launch_seed<9>, launch_seed<10>};
+
+long long steps_of(double h, double tmax) {
+  double q = std::nearbyint(tmax / h);  // round(Int64, tmax/h): ties to even
+  long long n = (long long)q;
+  return n < 0 ? -n : n;
+}
+// check_step (src/integrator/Integrator.jl:249-259)
+double check_step(double t0, double tmax) {
+  auto sgn = [](double x) { return x > 0 ? 1.0 : (x < 0 ? -1.0 : x); };
+  if (std::fabs(tmax) > std::fabs(t0)) return sgn(tmax);
+  if (sgn(tmax) != sgn(t0)) return sgn(tmax);
+  return -1.0 * sgn(tmax);
+}
+
+struct GroupPlan {
+  int N, grad;
+  unsigned long long kick;
+  std::vector<int> systems;  // global indices, longest first
+  long long max_steps = 0;
+};
+
+// Core of every entry point.  All array pointers are device pointers in the
+// caller's packed layout; desc / t0 / pair are host copies.
+int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const double* t_host,
+              const uint8_t* pair_host, double* d_t, double* d_x, double* d_v, const double* d_m, double* d_xe,
+              double* d_ve, double* d_J, double* d_E, double* d_dqdt, const double* d_jinit, double* d_tt,
+              double* d_dq0, double* d_dtdel, long long* d_count, uint32_t* status_host) {
+  cudaStream_t st = ctx->stream;
+  ctx->last_launches = 0;
+  ctx->last_orbit_ms = ctx->last_jac_ms = 0;
+  // ---- offsets and groups
+  std::vector<SysOff> off(nsys);
+  std::vector<long long> nsteps(nsys);
+  std::vector<double> hsig(nsys);
+  long long ax = 0, am = 0, aJ = 0, adq = 0, ap = 0, att = 0, adq0 = 0, acn = 0;
+  std::map<std::tuple<int, int, unsigned long long>, GroupPlan> groups;
+  for (int s = 0; s < nsys; s++) {
+    const nbg_system_desc& d = desc[s];
+    if (d.n < NBG_MIN_BODIES || d.n > NBG_MAX_BODIES)
+      return set_error(NBG_EUNSUPPORTED, "system %d: n = %d outside the built range %d..%d", s, d.n, NBG_MIN_BODIES,
+                       NBG_MAX_BODIES);
+    if (d.ti < 0 || d.ti >= d.n) return set_error(NBG_EINVAL, "system %d: ti = %d not in 0..%d", s, d.ti, d.n - 1);
+    if (d.ntt < 1) return set_error(NBG_EINVAL, "system %d: ntt = %d < 1", s, d.ntt);
+    if (!(d.h != 0.0) || !std::isfinite(d.h) || !std::isfinite(d.tmax))
+      return set_error(NBG_EINVAL, "system %d: h = %g, tmax = %g", s, d.h, d.tmax);
+    const int n = d.n, M = 7 * n;
+    SysOff& o = off[s];
+    o.x = ax; o.m = am; o.J = aJ; o.dqdt = adq; o.pair = ap; o.tt = att; o.dq = adq0; o.cnt = acn;
+    o.n = n; o.ntt = d.ntt; o.grad = d.grad ? 1 : 0; o.pad = 0;
+    ax += 3 * n; am += n; aJ += (long long)M * M; adq += M; ap += (long long)n * n;
+    att += (long long)n * d.ntt; adq0 += (long long)n * d.ntt * 7 * n; acn += n;
+    nsteps[s] = steps_of(d.h, d.tmax);
+    hsig[s] = d.h * check_step(t_host[s], d.tmax + t_host[s]);
+    unsigned long long kick = 0;
+    for (int i = 0; i < n - 1; i++)
+      for (int j = i + 1; j < n; j++)
+        if (pair_host[o.pair + i + (long long)n * j]) kick |= 1ull << pair_bit(i, j, n);
+    GroupPlan& gp = groups[std::make_tuple(n, o.grad, kick)];
+    gp.N = n; gp.grad = o.grad; gp.kick = kick;
+    gp.systems.push_back(s);
+    gp.max_steps = std::max(gp.max_steps, nsteps[s]);
+  }
+  SysOff* d_off;
+  int rc;
+  if ((rc = ctx->get("off", (size_t)nsys, &d_off))) return rc;
+  NBG_CUDA(cudaMemcpyAsync(d_off, off.data(), sizeof(SysOff) * nsys, cudaMemcpyHostToDevice, st));
+  long long* d_offtt;
+  long long* d_offdq;
+  if ((rc = ctx->get("offtt", (size_t)nsys, &d_offtt))) return rc;
+  if ((rc = ctx->get("offdq", (size_t)nsys, &d_offdq))) return rc;
+  {
+    std::vector<long long> a(nsys), b(nsys);
+    for (int s = 0; s < nsys; s++) { a[s] = off[s].tt; b[s] = off[s].dq; }
+    NBG_CUDA(cudaMemcpyAsync(d_offtt, a.data(), sizeof(long long) * nsys, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(d_offdq, b.data(), sizeof(long long) * nsys, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaStreamSynchronize(st));  // host vectors a, b go out of scope
+  }
+  const int K = std::max(1, ctx->chunk_steps);
+  // ---- per-group device state
+  std::vector<GroupArgs> gargs;
+  int* d_bad;
+  if ((rc = ctx->get("bad", 1, &d_bad))) return rc;
+  NBG_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(int), st));
+  int gi = 0;
+  std::vector<long long> gmaxsteps;
+  for (auto& kv : groups) {
+    GroupPlan& gp = kv.second;
+    std::stable_sort(gp.systems.begin(), gp.systems.end(),
+                     [&](int a, int b) { return nsteps[a] > nsteps[b]; });
+    const int N = gp.N, nsg = (int)gp.systems.size();
+    const int S = ((nsg + 31) / 32) * 32;
+    GroupArgs g;
+    memset(&g, 0, sizeof(g));
+    g.N = N; g.S = S; g.nsys = nsg; g.grad = gp.grad; g.K = K; g.kick = gp.kick;
+    int npk = 0;
+    for (int i = 0; i < N - 1; i++)
+      for (int j = i + 1; j < N; j++)
+        if (!((gp.kick >> pair_bit(i, j, N)) & 1)) npk++;
+    g.npk = npk;
+    g.R = step_record_size(N, npk, gp.kick != 0);
+    char nm[64];
+    auto name = [&](const char* f) { snprintf(nm, sizeof(nm), "g%d_%s", gi, f); return nm; };
+#define GET(field, cnt) if ((rc = ctx->get(name(#field), (size_t)(cnt), &g.field))) return rc
+    GET(x, 3 * N * S); GET(v, 3 * N * S); GET(xe, 3 * N * S); GET(ve, 3 * N * S); GET(m, N * S);
+    GET(dqdt, 7 * N * S); GET(gsave, N * S); GET(count, N * S); GET(t0, S); GET(h, S); GET(hI, S);
+    GET(nsteps, S); GET(ntt, S); GET(ti, S); GET(sysidx, S); GET(status, S);
+    if (gp.grad) {
+      GET(steprec, (size_t)K * g.R * S); GET(trec, (size_t)K * (N - 1) * (7 * N + 1) * S);
+      GET(tflag, (size_t)K * (N - 1) * S); GET(scratch, (size_t)g.R * S);
+      GET(Jint, (size_t)S * 6 * N * 7 * N); GET(Eint, (size_t)S * 6 * N * 7 * N);
+    }
+#undef GET
+    g.tt = d_tt; g.off_tt = d_offtt; g.dtdq0 = d_dq0; g.off_dq = d_offdq;
+    // host-side scalars
+    std::vector<int> sidx(S, -1), vntt(S, 1), vti(S, 0);
+    std::vector<double> vt0(S, 0.0), vh(S, 0.0), vhI(S, 0.0);
+    std::vector<long long> vns(S, 0);
+    for (int q = 0; q < nsg; q++) {
+      int s = gp.systems[q];
+      sidx[q] = s; vntt[q] = desc[s].ntt; vti[q] = desc[s].ti;
+      vt0[q] = t_host[s]; vh[q] = hsig[s]; vhI[q] = desc[s].h; vns[q] = nsteps[s];
+    }
+    NBG_CUDA(cudaMemcpyAsync(g.sysidx, sidx.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(g.ntt, vntt.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(g.ti, vti.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(g.t0, vt0.data(), sizeof(double) * S, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(g.h, vh.data(), sizeof(double) * S, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(g.hI, vhI.data(), sizeof(double) * S, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(g.nsteps, vns.data(), sizeof(long long) * S, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaMemsetAsync(g.status, 0, sizeof(unsigned) * S, st));
+    NBG_CUDA(cudaStreamSynchronize(st));
+    // gather state
+    int pb = (S + 127) / 128;
+    pack_state_kernel<<<pb, 128, 0, st>>>(N, S, g.sysidx, d_off, d_x, d_v, d_xe, d_ve, d_m, d_dqdt, d_count, g.x,
+                                          g.v, g.xe, g.ve, g.m, g.dqdt, g.count);
+    ctx->last_launches++;
+    if (gp.grad) {
+      long long tot = (long long)S * 49 * N * N;
+      pack_jac_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(N, S, g.sysidx, d_off, d_J, d_E, g.Jint, g.Eint,
+                                                                     d_bad);
+      ctx->last_launches++;
+    }
+    gargs.push_back(g);
+    gmaxsteps.push_back(gp.max_steps);
+    gi++;
+  }
+  NBG_CUDA(cudaGetLastError());
+  int bad = 0;
+  NBG_CUDA(cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaStreamSynchronize(st));
+  if (bad)
+    return set_error(NBG_EUNSUPPORTED,
+                     "jac_step mass rows must be unit rows with zero jac_error (true for every State the reference "
+                     "builds and integrates)");
+  for (auto& g : gargs) {
+    kSeed[g.N](g, st);
+    ctx->last_launches++;
+  }
+  // ---- chunk loop
+  long long max_steps = 0;
+  for (auto& kv : groups) max_steps = std::max(max_steps, kv.second.max_steps);
+  const long long nchunks = (max_steps + K - 1) / K;
+  NBG_CUDA(cudaEventRecord(ctx->ev0, st));
+  for (long long c = 0; c < nchunks; c++) {
+    for (size_t q = 0; q < gargs.size(); q++) {
+      const GroupArgs& g = gargs[q];
+      if (c * K >= gmaxsteps[q]) continue;
+      kOrbit[g.N](g, (int)c, st);
+      ctx->last_launches++;
+      if (g.grad) {
+        kJac[g.N](g, (int)c, st);
+        ctx->last_launches++;
+      }
+    }
+  }
+  NBG_CUDA(cudaGetLastError());
+  NBG_CUDA(cudaEventRecord(ctx->ev1, st));
+  // ---- outputs
+  for (auto& g : gargs) {
+    int pb = (g.S + 127) / 128;
+    unpack_state_kernel<<<pb, 128, 0, st>>>(g.N, g.S, g.grad, g.sysidx, d_off, d_x, d_v, d_xe, d_ve, d_dqdt, d_count,
+                                            g.x, g.v, g.xe, g.ve, g.dqdt, g.count);
+    ctx->last_launches++;
+    if (g.grad) {
+      long long tot = (long long)g.S * 42 * g.N * g.N;
+      unpack_jac_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.N, g.S, g.sysidx, d_off, d_J, d_E, g.Jint,
+                                                                       g.Eint);
+      ctx->last_launches++;
+    }
+  }
+  {
+    dim3 grid(8, std::min(nsys, 65535), (nsys + 65534) / 65535);
+    dtdelements_kernel<<<grid, 256, 0, st>>>(nsys, d_off, d_dq0, d_jinit, d_dtdel, d_count);
+    ctx->last_launches++;
+  }
+  // s.t = t0 + nsteps * h (Transits.jl:161 at the last step)
+  {
+    std::vector<double> tout(nsys);
+    for (int s = 0; s < nsys; s++) tout[s] = nsteps[s] > 0 ? t_host[s] + (double)nsteps[s] * hsig[s] : t_host[s];
+    NBG_CUDA(cudaMemcpyAsync(d_t, tout.data(), sizeof(double) * nsys, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaStreamSynchronize(st));
+  }
+  NBG_CUDA(cudaGetLastError());
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  ctx->last_total_ms = ms;
+  if (status_host) {
+    std::fill(status_host, status_host + nsys, 0u);
+    for (auto& g : gargs) {
+      std::vector<unsigned> sv(g.S);
+      std::vector<int> si(g.S);
+      NBG_CUDA(cudaMemcpy(sv.data(), g.status, sizeof(unsigned) * g.S, cudaMemcpyDeviceToHost));
+      NBG_CUDA(cudaMemcpy(si.data(), g.sysidx, sizeof(int) * g.S, cudaMemcpyDeviceToHost));
+      for (int q = 0; q < g.S; q++)
+        if (si[q] >= 0) status_host[si[q]] = sv[q];
+    }
+  }
+  return NBG_OK;
+}
+
+}  // namespace
+
+// ===================================================================== C ABI
+
+extern "C" {
+
+int nbg_version(void) { return 100; }
+
+int nbg_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return NBG_EINVAL;
+  snprintf(buf, len, "%s", g_last_error.c_str());
+  return NBG_OK;
+}
+
+int nbg_device_info(int device, nbg_device_info_t* out) {
+  if (!out) return set_error(NBG_EINVAL, "out is NULL");
+  cudaDeviceProp p;
+  NBG_CUDA(cudaGetDeviceProperties(&p, device));
+  memset(out, 0, sizeof(*out));
+  snprintf(out->name, sizeof(out->name), "%s", p.name);
+  out->sm_count = p.multiProcessorCount;
+  out->cc_major = p.major;
+  out->cc_minor = p.minor;
+  out->total_mem = p.totalGlobalMem;
+  out->min_bodies = NBG_MIN_BODIES;
+  out->max_bodies = NBG_MAX_BODIES;
+  return NBG_OK;
+}
+
+int nbg_create(int device, nbg_context** out) {
+  if (!out) return set_error(NBG_EINVAL, "out is NULL");
+  *out = nullptr;
+  int ndev = 0;
+  NBG_CUDA(cudaGetDeviceCount(&ndev));
+  if (device < 0 || device >= ndev) return set_error(NBG_EINVAL, "device %d not in 0..%d", device, ndev - 1);
+  NBG_CUDA(cudaSetDevice(device));
+  nbg_context* c = new nbg_context();
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+    delete c;
+    return set_error(NBG_ECUDA, "stream/event creation failed");
+  }
+  *out = c;
+  return NBG_OK;
+}
+
+int nbg_destroy(nbg_context* ctx) {
+  if (!ctx) return NBG_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& kv : ctx->pool)
+    if (kv.second.p) cudaFree(kv.second.p);
+  cudaEventDestroy(ctx->ev0);
+  cudaEventDestroy(ctx->ev1);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return NBG_OK;
+}
+
+int nbg_set_tuning(nbg_context* ctx, int chunk_steps, int overlap) {
+  if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
+  if (chunk_steps < 0 || chunk_steps > 4096) return set_error(NBG_EINVAL, "chunk_steps = %d", chunk_steps);
+  if (chunk_steps) ctx->chunk_steps = chunk_steps;
+  if (overlap >= 0) ctx->overlap = overlap;
+  return NBG_OK;
+}
+
+int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double* jacobian_ms) {
+  if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
+  if (total_ms) *total_ms = ctx->last_total_ms;
+  if (orbit_ms) *orbit_ms = ctx->last_orbit_ms;
+  if (jacobian_ms) *jacobian_ms = ctx->last_jac_ms;
+  return NBG_OK;
+}
+
+int64_t nbg_last_launch_count(nbg_context* ctx) { return ctx ? ctx->last_launches : -1; }
+
+static int batch_host_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc, double* t, double* x,
+                             double* v, const double* m, double* xerror, double* verror, double* jac_step,
+                             double* jac_error, double* dqdt, const uint8_t* pair, const double* jac_init, double* tt,
+                             double* dtdq0, double* dtdelements, int64_t* count, uint32_t* status, bool copy_outputs_in) {
+  if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
+  if (nsys <= 0 || !desc) return set_error(NBG_EINVAL, "nsys = %d", nsys);
+  NBG_CUDA(cudaSetDevice(ctx->device));
+  long long ax = 0, am = 0, aJ = 0, adq = 0, ap = 0, att = 0, adq0 = 0;
+  for (int s = 0; s < nsys; s++) {
+    int n = desc[s].n, M = 7 * n;
+    if (n < NBG_MIN_BODIES || n > NBG_MAX_BODIES)
+      return set_error(NBG_EUNSUPPORTED, "system %d: n = %d outside %d..%d", s, n, NBG_MIN_BODIES, NBG_MAX_BODIES);
+    if (desc[s].ntt < 1) return set_error(NBG_EINVAL, "system %d: ntt = %d", s, desc[s].ntt);
+    ax += 3 * n; am += n; aJ += (long long)M * M; adq += M; ap += (long long)n * n;
+    att += (long long)n * desc[s].ntt; adq0 += (long long)n * desc[s].ntt * 7 * n;
+  }
+  if (!copy_outputs_in)
+    for (long long q = 0; q < am; q++)
+      if (count[q] != 0) return set_error(NBG_EINVAL, "batched calls need fresh TransitTiming outputs (count == 0)");
+  cudaStream_t st = ctx->stream;
+  double *d_t, *d_x, *d_v, *d_m, *d_xe, *d_ve, *d_J, *d_E, *d_dq, *d_ji, *d_tt, *d_dq0, *d_del;
+  long long* d_cnt;
+  int rc;
+#define GETB(ptr, nm, cnt) if ((rc = ctx->get(nm, (size_t)(cnt), &ptr))) return rc
+  GETB(d_t, "u_t", nsys); GETB(d_x, "u_x", ax); GETB(d_v, "u_v", ax); GETB(d_m, "u_m", am);
+  GETB(d_xe, "u_xe", ax); GETB(d_ve, "u_ve", ax); GETB(d_J, "u_J", aJ); GETB(d_E, "u_E", aJ);
+  GETB(d_dq, "u_dq", adq); GETB(d_ji, "u_ji", aJ); GETB(d_tt, "u_tt", att); GETB(d_dq0, "u_dq0", adq0);
+  GETB(d_del, "u_del", adq0); GETB(d_cnt, "u_cnt", am);
+#undef GETB
+  NBG_CUDA(cudaMemcpyAsync(d_t, t, sizeof(double) * nsys, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_x, x, sizeof(double) * ax, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_v, v, sizeof(double) * ax, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_m, m, sizeof(double) * am, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_xe, xerror, sizeof(double) * ax, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_ve, verror, sizeof(double) * ax, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_J, jac_step, sizeof(double) * aJ, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_E, jac_error, sizeof(double) * aJ, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_dq, dqdt, sizeof(double) * adq, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_ji, jac_init, sizeof(double) * aJ, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_cnt, count, sizeof(long long) * am, cudaMemcpyHostToDevice, st));
+  if (copy_outputs_in) {
+    NBG_CUDA(cudaMemcpyAsync(d_tt, tt, sizeof(double) * att, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(d_dq0, dtdq0, sizeof(double) * adq0, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(d_del, dtdelements, sizeof(double) * adq0, cudaMemcpyHostToDevice, st));
+  } else {
+    NBG_CUDA(cudaMemsetAsync(d_tt, 0, sizeof(double) * att, st));
+    NBG_CUDA(cudaMemsetAsync(d_dq0, 0, sizeof(double) * adq0, st));
+    NBG_CUDA(cudaMemsetAsync(d_del, 0, sizeof(double) * adq0, st));
+  }
+  rc = run_batch(ctx, nsys, desc, t, pair, d_t, d_x, d_v, d_m, d_xe, d_ve, d_J, d_E, d_dq, d_ji, d_tt, d_dq0, d_del,
+                 d_cnt, status);
+  if (rc) return rc;
+  NBG_CUDA(cudaMemcpyAsync(t, d_t, sizeof(double) * nsys, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(x, d_x, sizeof(double) * ax, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(v, d_v, sizeof(double) * ax, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(xerror, d_xe, sizeof(double) * ax, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(verror, d_ve, sizeof(double) * ax, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(jac_step, d_J, sizeof(double) * aJ, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(jac_error, d_E, sizeof(double) * aJ, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(dqdt, d_dq, sizeof(double) * adq, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(count, d_cnt, sizeof(long long) * am, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(tt, d_tt, sizeof(double) * att, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(dtdq0, d_dq0, sizeof(double) * adq0, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(dtdelements, d_del, sizeof(double) * adq0, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaStreamSynchronize(st));
+  return NBG_OK;
+}
+
+int nbg_integrate_transits(nbg_context* ctx, int n, int ti, double h, double tmax, int grad, double* t, double* x,
+                           double* v, const double* m, double* xerror, double* verror, double* jac_step,
+                           double* jac_error, double* dqdt, const uint8_t* pair, const double* jac_init, int64_t ntt,
+                           double* tt, double* dtdq0, double* dtdelements, int64_t* count) {
+  if (!t || !x || !v || !m || !xerror || !verror || !jac_step || !jac_error || !dqdt || !pair || !jac_init || !tt ||
+      !dtdq0 || !dtdelements || !count)
+    return set_error(NBG_EINVAL, "NULL array argument");
+  if (ntt < 1 || ntt > (1LL << 30)) return set_error(NBG_EINVAL, "ntt = %lld", (long long)ntt);
+  nbg_system_desc d;
+  d.n = n; d.ti = ti; d.grad = grad ? 1 : 0; d.ntt = (int32_t)ntt; d.h = h; d.tmax = tmax;
+  if (n < NBG_MIN_BODIES || n > NBG_MAX_BODIES)
+    return set_error(NBG_EUNSUPPORTED, "n = %d outside %d..%d", n, NBG_MIN_BODIES, NBG_MAX_BODIES);
+  if (ti < 0 || ti >= n) return set_error(NBG_EINVAL, "ti = %d not in 0..%d", ti, n - 1);
+  return batch_host_device(ctx, 1, &d, t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair, jac_init, tt,
+                           dtdq0, dtdelements, count, nullptr, true);
+}
+
+int nbg_batch_integrate_transits(nbg_context* ctx, int nsys, const nbg_system_desc* desc, double* t, double* x,
+                                 double* v, const double* m, double* xerror, double* verror, double* jac_step,
+                                 double* jac_error, double* dqdt, const uint8_t* pair, const double* jac_init,
+                                 double* tt, double* dtdq0, double* dtdelements, int64_t* count, uint32_t* status) {
+  return batch_host_device(ctx, nsys, desc, t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair, jac_init, tt,
+                           dtdq0, dtdelements, count, status, false);
+}
+
+int nbg_batch_integrate_transits_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc, double* t,
+                                        double* x, double* v, const double* m, double* xerror, double* verror,
+                                        double* jac_step, double* jac_error, double* dqdt, const uint8_t* pair,
+                                        const double* jac_init, double* tt, double* dtdq0, double* dtdelements,
+                                        int64_t* count, uint32_t* status) {
+  if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
+  if (nsys <= 0 || !desc) return set_error(NBG_EINVAL, "nsys = %d", nsys);
+  NBG_CUDA(cudaSetDevice(ctx->device));
+  // the orchestration needs start times and pair flags on the host
+  long long ap = 0;
+  for (int s = 0; s < nsys; s++) {
+    if (desc[s].n < NBG_MIN_BODIES || desc[s].n > NBG_MAX_BODIES)
+      return set_error(NBG_EUNSUPPORTED, "system %d: n = %d", s, desc[s].n);
+    ap += (long long)desc[s].n * desc[s].n;
+  }
+  std::vector<double> th(nsys);
+  std::vector<uint8_t> ph(ap);
+  NBG_CUDA(cudaMemcpy(th.data(), t, sizeof(double) * nsys, cudaMemcpyDeviceToHost));
+  NBG_CUDA(cudaMemcpy(ph.data(), pair, ap, cudaMemcpyDeviceToHost));
+  return run_batch(ctx, nsys, desc, th.data(), ph.data(), t, x, v, m, xerror, verror, jac_step, jac_error, dqdt,
+                   jac_init, tt, dtdq0, dtdelements, (long long*)count, status);
+}
+
+}  // extern "C"

@@ -1,0 +1,148 @@
+// nbg_jacobian.cuh -- the Jacobian consumer: one GPU lane owns one column of
+// jac_step (and of jac_error) of one system and applies the operator stream
+// the orbit producer recorded, with the reference's compensated summation.
+//
+// Every update of ahl21! on jac_step (src/integrator/ahl21/ahl21.jl:5-95) has
+// the form J <- J + A J followed by comp_sum_matrix!(J, J_err, A J)
+// (src/utils.jl:36-46); columns of J never mix, so a column is a complete
+// unit of work.  The consumer keeps the 6N non-mass rows of its column in
+// shared memory ([row][lane], conflict-free); the mass rows of J are unit
+// rows that no operator touches (the library checks this on entry).
+//
+// The pair update uses the structure of jac_ij (ahl21.jl:734-750): rows of
+// body i are mj*K, -mj*K on (x,v)_i, (x,v)_j and rows of body j are -mi*K,
+// mi*K, so jac_ij * [J_i; J_j] = [mj u; -mi u] with u = K (J_i - J_j), plus
+// the two mass columns.  That is 54 FP64 operations per column instead of
+// 144 for the dense 12x12 block; the product is rounded differently from a
+// dense BLAS product, which the reference's BLAS leaves unspecified anyway.
+#pragma once
+#include "nbg_orbit.cuh"
+
+namespace nbg {
+
+// Kahan fold with a zero addend (comp_sum_matrix! on a zero entry).
+__device__ __forceinline__ void fold(double& s, double& e) {
+  double t = s + e;
+  e = (s - t) + e;
+  s = t;
+}
+
+// P[vr] = (A J)[velocity row vr] for the compact operator at record offset
+// roff: the FMA chain of the dense product in the reference's column order,
+// with the exact no-op terms (zero operator entries; mass rows of J, which
+// are unit rows) reduced to the single mass entry of this column.
+template <int N, int BS>
+__device__ __forceinline__ void op_product(const double* J, const Rec& rec, int roff, int c, double* P) {
+  const int cm = (c % 7 == 6) ? c / 7 : -1;  // body whose mass this column is
+#pragma unroll 1
+  for (int vr = 0; vr < 3 * N; vr++) {
+    const int rb = roff + vr * (4 * N);
+    double acc = 0.0;
+#pragma unroll
+    for (int d = 0; d < N; d++) {
+#pragma unroll
+      for (int p = 0; p < 3; p++) acc = fma(rec.get(rb + 4 * d + p), J[(6 * d + p) * BS], acc);
+      if (d == cm) acc = acc + rec.get(rb + 4 * d + 3);
+    }
+    P[vr] = acc;
+  }
+}
+
+// One Kepler pair block update (ahl21.jl:31-42 / :64-75) on this column.
+template <int N, int BS>
+__device__ __forceinline__ void pair_apply(double* J, double* E, int c, int i, int j, const Rec& rec, int roff) {
+  double D[6];
+#pragma unroll
+  for (int l = 0; l < 6; l++) D[l] = J[(6 * i + l) * BS] - J[(6 * j + l) * BS];
+  const double mi = rec.get(roff + PREC_MI), mj = rec.get(roff + PREC_MJ);
+  const bool ci = (c == 7 * i + 6), cj = (c == 7 * j + 6);
+#pragma unroll
+  for (int r = 0; r < 6; r++) {
+    double u = rec.get(roff + r * 6) * D[0];
+#pragma unroll
+    for (int l = 1; l < 6; l++) u = fma(rec.get(roff + r * 6 + l), D[l], u);
+    double ai = mj * u, aj = (-mi) * u;
+    if (ci) {
+      ai = ai + rec.get(roff + PREC_MC6 + r);
+      aj = aj + rec.get(roff + PREC_MC6 + 6 + r);
+    }
+    if (cj) {
+      ai = ai + rec.get(roff + PREC_MC13 + r);
+      aj = aj + rec.get(roff + PREC_MC13 + 6 + r);
+    }
+    kahan(J[(6 * i + r) * BS], E[(6 * i + r) * BS], ai);
+    kahan(J[(6 * j + r) * BS], E[(6 * j + r) * BS], aj);
+  }
+}
+
+// J <- J + A J on all non-mass rows: velocity rows take the product P,
+// position rows a zero addend.
+template <int N, int BS>
+__device__ __forceinline__ void add_velocity_rows(double* J, double* E, const double* P) {
+#pragma unroll 1
+  for (int b = 0; b < N; b++) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) fold(J[(6 * b + k) * BS], E[(6 * b + k) * BS]);
+#pragma unroll
+    for (int k = 0; k < 3; k++) kahan(J[(6 * b + 3 + k) * BS], E[(6 * b + 3 + k) * BS], P[3 * b + k]);
+  }
+}
+template <int N, int BS>
+__device__ __forceinline__ void fold_all(double* J, double* E) {
+#pragma unroll 1
+  for (int b = 0; b < N; b++)
+#pragma unroll
+    for (int r = 0; r < 6; r++) fold(J[(6 * b + r) * BS], E[(6 * b + r) * BS]);
+}
+
+// drift_grad! on jac_step (ahl21.jl:318-331): x rows += h * v rows.
+template <int N, int BS>
+__device__ __forceinline__ void drift_rows(double* J, double* E, double h) {
+#pragma unroll 1
+  for (int b = 0; b < N; b++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) kahan(J[(6 * b + k) * BS], E[(6 * b + k) * BS], h * J[(6 * b + 3 + k) * BS]);
+}
+
+// One recorded step on this column (ahl21.jl:5-95, the jac_step updates).
+template <int N, int BS>
+__device__ void apply_step(double* J, double* E, int c, double h, uint64_t kick, const Rec& rec) {
+  const double h2 = 0.5 * h;
+  double P[3 * N];
+  int roff = 0;
+  if (kick) {
+    op_product<N, BS>(J, rec, roff, c, P);  // jac_kick * jac_step before the drift
+    roff += op_size(N);
+  }
+  drift_rows<N, BS>(J, E, h2);
+  if (kick) add_velocity_rows<N, BS>(J, E, P);
+  else fold_all<N, BS>(J, E);
+#pragma unroll 1
+  for (int i = 0; i < N - 1; i++)
+#pragma unroll 1
+    for (int j = i + 1; j < N; j++) {
+      if ((kick >> pair_bit(i, j, N)) & 1) continue;
+      pair_apply<N, BS>(J, E, c, i, j, rec, roff);
+      roff += PREC;
+    }
+  op_product<N, BS>(J, rec, roff, c, P);
+  roff += op_size(N);
+  add_velocity_rows<N, BS>(J, E, P);
+#pragma unroll 1
+  for (int i = N - 2; i >= 0; i--)
+#pragma unroll 1
+    for (int j = N - 1; j > i; j--) {
+      if ((kick >> pair_bit(i, j, N)) & 1) continue;
+      pair_apply<N, BS>(J, E, c, i, j, rec, roff);
+      roff += PREC;
+    }
+  drift_rows<N, BS>(J, E, h2);
+  if (kick) {
+    op_product<N, BS>(J, rec, roff, c, P);
+    add_velocity_rows<N, BS>(J, E, P);
+  } else {
+    fold_all<N, BS>(J, E);
+  }
+}
+
+}  // namespace nbg

@@ -1,0 +1,465 @@
+// nbg_kepler.cuh -- device-side universal-variable Kepler drift for one body
+// pair and its analytic Jacobian, FP64.
+//
+// Restates, for one lane = one system, NbodyGradient.jl's
+//   jac_delxv_gamma!        src/integrator/ahl21/ahl21.jl:766-890
+//   compute_jacobian_gamma! src/integrator/ahl21/ahl21.jl:896-1139
+//   cubic1, G3, H1, H2, H3, H5, H6 and their series  src/utils.jl:103-396
+// The translation unit is compiled with --fmad=false: every product and sum
+// rounds on its own, as Julia evaluates them; fma() appears only where the
+// reference itself takes a fused product (Base.:^(x, 4)).
+//
+// GPU-specific structure: the six G/H series share one fused loop (each
+// series still runs its own recurrence and stops on its own exact-equality
+// test, so values are those of the separate loops) which turns six dependent
+// FP64 division chains into independent ones the scheduler can overlap.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nbg {
+
+// src/NbodyGradient.jl:13-17
+constexpr double GNEWT = 39.4845 / (365.242 * 365.242);
+constexpr double THIRD = 1.0 / 3.0;
+
+__device__ __forceinline__ double jsign(double x) { return x > 0.0 ? 1.0 : (x < 0.0 ? -1.0 : x); }
+
+// comp_sum (src/utils.jl:16-23)
+__device__ __forceinline__ void kahan(double& s, double& e, double a) {
+  e = e + a;
+  double t = s + e;
+  e = (s - t) + e;
+  s = t;
+}
+
+// Base.:^(x::Float64, 4): compensated power by squaring
+__device__ __forceinline__ double pow4(double x) {
+  double x2 = x * x;
+  double x2lo = fma(x, x, -x2);
+  double err = x2 * 2.0 * x2lo;
+  double x4 = x2 * x2;
+  double x4lo = fma(x2, x2, -x4);
+  double lo = x4lo + err;
+  if (isfinite(x4) && isfinite(lo)) return x4 + lo;
+  return x4;
+}
+
+// cubic1 (src/utils.jl:103-122)
+__device__ __forceinline__ double cubic1(double a, double b, double c) {
+  double a3 = a * THIRD;
+  double Q = a3 * a3 - b * THIRD;
+  double R = a3 * a3 * a3 + 0.5 * ((-a3) * b + c);
+  double R2 = R * R, Q3 = Q * Q * Q;
+  if (R2 < Q3) return -c / b;
+  double A = (-jsign(R)) * cbrt(fabs(R) + sqrt(R2 - Q3));
+  double B = (A == 0.0) ? 0.0 : Q / A;
+  return A + B - a3;
+}
+
+enum : int { GH_G3 = 1, GH_H1 = 2, GH_H2 = 4, GH_H3 = 8, GH_H5 = 16, GH_H6 = 32 };
+
+struct GH {
+  double g3, h1, h2, h3, h5, h6;
+};
+
+// G3, H1, H2, H3, H5, H6 at (gamma, beta) -- the subset named by NEED.
+// gamma < 0.5: series (utils.jl:137-165, 180-209, 225-254, 271-303, 320-349,
+// 364-396) advanced in one loop; otherwise the closed forms of utils.jl.
+template <int NEED>
+__device__ __forceinline__ GH gh_functions(double gamma, double beta, double sqb) {
+  GH o;
+  o.g3 = o.h1 = o.h2 = o.h3 = o.h5 = o.h6 = 0.0;
+  if (gamma < 0.5) {
+    double x2 = (-jsign(beta)) * (gamma * gamma);
+    double tg = 1.0, g3 = 1.0, g31 = 2.0, g32 = 2.0;
+    double t1 = 1.0, h1 = 1.0, h11 = 2.0, h12 = 2.0;
+    double t2 = 1.0, h2 = 1.0, h21 = 2.0, h22 = 2.0;
+    double t3 = 1.0 / 30.0, h3 = 1.0 / 10.0, h31 = 2.0 * h3, h32 = 2.0 * h3, f3 = 4.0;
+    double t5 = 1.0 / 60.0, h5 = t5, h51 = 2.0 * h5, h52 = 2.0 * h5;
+    double t6 = 1.0 / 360.0, h6 = 1.0 / 40.0, h61 = 2.0 * h6, h62 = 2.0 * h6, f6 = 16.0;
+    bool dg = !(NEED & GH_G3), d1 = !(NEED & GH_H1), d2 = !(NEED & GH_H2);
+    bool d3 = !(NEED & GH_H3), d5 = !(NEED & GH_H5), d6 = !(NEED & GH_H6);
+    for (int n = 1; n <= 100; n++) {
+      if (!dg) {
+        g32 = g31; g31 = g3;
+        tg = tg * (x2 / (double)((2 * n + 3) * (2 * n + 2)));
+        g3 = g3 + tg;
+        dg = (n >= 100) || g3 == g32 || g3 == g31;
+      }
+      if (!d1) {
+        h12 = h11; h11 = h1;
+        t1 = t1 * (x2 * (double)(n + 1));
+        t1 = t1 / (double)((2 * n + 4) * (2 * n + 3) * n);
+        h1 = h1 + t1;
+        d1 = (n >= 100) || h1 == h12 || h1 == h11;
+      }
+      if (!d2) {
+        h22 = h21; h21 = h2;
+        t2 = t2 * x2;
+        t2 = t2 / (double)((4 * n + 6) * n);
+        h2 = h2 + t2;
+        d2 = (n >= 100) || h2 == h22 || h2 == h21;
+      }
+      if (!d3) {
+        h32 = h31; h31 = h3;
+        t3 = t3 * x2;
+        t3 = t3 / (double)((2 * n + 4) * (2 * n + 5));
+        f3 = f3 * 4.0;
+        h3 = h3 + t3 * (f3 - 1.0);
+        d3 = (n >= 100) || h3 == h32 || h3 == h31;
+      }
+      if (!d5) {
+        h52 = h51; h51 = h5;
+        t5 = t5 * (x2 * (double)(n + 1));
+        t5 = t5 / (double)((2 * n + 5) * (2 * n + 4) * n);
+        h5 = h5 + t5;
+        d5 = (n >= 100) || h5 == h52 || h5 == h51;
+      }
+      if (!d6) {
+        h62 = h61; h61 = h6;
+        t6 = t6 * x2;
+        t6 = t6 / (double)((2 * n + 5) * (2 * n + 6));
+        f6 = f6 * 4.0;
+        h6 = h6 + t6 * (f6 - (double)(3 * n) - 7.0);
+        d6 = (n >= 100) || h6 == h62 || h6 == h61;
+      }
+      if (dg && d1 && d2 && d3 && d5 && d6) break;
+    }
+    if (NEED & GH_G3) o.g3 = g3 * (((-x2) * gamma) / ((6.0 * beta) * sqb));
+    if (NEED & GH_H1) o.h1 = h1 * ((x2 * x2) / (12.0 * (beta * beta)));
+    if (NEED & GH_H2) o.h2 = h2 * (((-x2) * gamma) / ((3.0 * beta) * sqb));
+    if (NEED & GH_H3) o.h3 = h3 * (((-(x2 * x2)) * gamma) / (beta * sqb));
+    if (NEED & GH_H5) o.h5 = h5 * (((-(x2 * x2)) * gamma) / (beta * sqb));
+    if (NEED & GH_H6) o.h6 = h6 * ((-(x2 * x2 * x2)) / (beta * beta));
+  } else if (beta >= 0.0) {
+    double s, c;
+    sincos(gamma, &s, &c);
+    if (NEED & GH_G3) o.g3 = (gamma - s) / (sqb * beta);
+    if (NEED & GH_H1) {
+      double sh = sin(0.5 * gamma);
+      o.h1 = (4.0 * (sh * sh) - gamma * s) / (beta * beta);
+    }
+    if (NEED & GH_H2) o.h2 = (s - gamma * c) / (sqb * beta);
+    if (NEED & GH_H3) o.h3 = (4.0 * s - s * c - 3.0 * gamma) / (beta * sqb);
+    if (NEED & GH_H5) o.h5 = (3.0 * s - 2.0 * gamma - gamma * c) / (beta * sqb);
+    if (NEED & GH_H6) o.h6 = (9.0 - 8.0 * c - cos(2.0 * gamma) - (6.0 * gamma) * s) / (2.0 * (beta * beta));
+  } else {
+    double s = sinh(gamma), c = cosh(gamma);
+    if (NEED & GH_G3) o.g3 = (gamma - s) / (sqb * beta);
+    if (NEED & GH_H1) {
+      double sh = sinh(0.5 * gamma);
+      o.h1 = (-4.0 * (sh * sh) + gamma * s) / (beta * beta);
+    }
+    if (NEED & GH_H2) o.h2 = (s - gamma * c) / (sqb * beta);
+    if (NEED & GH_H3) o.h3 = (4.0 * s - s * c - 3.0 * gamma) / (beta * sqb);
+    if (NEED & GH_H5) o.h5 = (3.0 * s - 2.0 * gamma - gamma * c) / (beta * sqb);
+    if (NEED & GH_H6) o.h6 = (9.0 - 8.0 * c - cosh(2.0 * gamma) + (6.0 * gamma) * s) / (2.0 * (beta * beta));
+  }
+  return o;
+}
+
+// Parameters jac_delxv_gamma! hands to compute_jacobian_gamma! (ahl21.jl:888)
+// plus the H values the Jacobian needs.
+struct KepParams {
+  double gamma, g0, g1, g2, g3, h1, h2, dfdt, fm1, gmh, dgdtm1, r0, r, r0inv, rinv, k, h, beta, betainv, eta, sqb,
+      zeta;
+  double H1v, H2v, H3v, H5v, H6v;
+  int newton_iter;
+};
+
+// jac_delxv_gamma! (ahl21.jl:766-890): Kepler drift of the relative orbit
+// (x0, v0) with k = G (m_i + m_j) over h; writes delxv (position and velocity
+// differences, finish - start minus the drift terms).
+template <bool DRIFT_FIRST, bool JAC>
+__device__ __noinline__ void kep_delxv(const double* x0, const double* v0, double k, double h, double* delxv,
+                                          KepParams& P) {
+  double rt0 = x0[0] - h * v0[0], rt1 = x0[1] - h * v0[1], rt2 = x0[2] - h * v0[2];
+  double r0 = DRIFT_FIRST ? sqrt(rt0 * rt0 + rt1 * rt1 + rt2 * rt2) : sqrt(x0[0] * x0[0] + x0[1] * x0[1] + x0[2] * x0[2]);
+  double r0inv = 1.0 / r0;
+  double beta0 = 2.0 * k * r0inv - (v0[0] * v0[0] + v0[1] * v0[1] + v0[2] * v0[2]);
+  double beta0inv = 1.0 / beta0;
+  double signb = jsign(beta0);
+  double sqb = sqrt(signb * beta0);
+  double zeta = k - r0 * beta0;
+  double eta = DRIFT_FIRST ? (rt0 * v0[0] + rt1 * v0[1] + rt2 * v0[2]) : (x0[0] * v0[0] + x0[1] * v0[1] + x0[2] * v0[2]);
+  double gamma_guess;
+  if (zeta != 0.0) {
+    double zinv = 6.0 / zeta;
+    gamma_guess = cubic1(0.5 * eta * sqb * zinv, r0 * signb * beta0 * zinv, (-h) * signb * beta0 * sqb * zinv);
+  } else if (eta != 0.0) {
+    double reta = r0 / eta;
+    double disc = reta * reta + 2.0 * h / eta;
+    gamma_guess = (disc > 0.0) ? sqb * ((-reta) + sqrt(disc)) : h * r0inv * sqb;
+  } else {
+    gamma_guess = h * r0inv * sqb;
+  }
+  double gamma = gamma_guess;
+  double gamma1 = 2.0 * gamma, gamma2 = 3.0 * gamma;
+  double c2 = -2.0 * zeta, c3 = 2.0 * eta * signb * sqb, c4 = (-sqb) * h * beta0, c5 = 2.0 * eta * signb * sqb;
+  double sx, cx;
+  int iter = 0;
+  while (iter < 20) {
+    gamma2 = gamma1;
+    gamma1 = gamma;
+    double xx = 0.5 * gamma;
+    if (beta0 > 0.0) {
+      sincos(xx, &sx, &cx);
+    } else {
+      sx = sinh(xx);
+      cx = exp(-xx) + sx;
+    }
+    gamma = gamma - (k * gamma + c2 * sx * cx + c3 * (sx * sx) + c4) /
+                        (2.0 * signb * zeta * (sx * sx) + c5 * sx * cx + r0 * beta0);
+    iter += 1;
+    if (gamma == gamma2 || gamma == gamma1) break;
+  }
+  P.newton_iter = iter;
+  double xx = 0.5 * gamma;
+  if (beta0 > 0.0) {
+    sincos(xx, &sx, &cx);
+  } else {
+    sx = sinh(xx);
+    cx = exp(-xx) + sx;
+  }
+  double g1bs = 2.0 * sx * cx / sqb;
+  double g2bs = 2.0 * signb * (sx * sx) * beta0inv;
+  double g0bs = 1.0 - beta0 * g2bs;
+  constexpr int NEED = JAC ? (GH_G3 | GH_H1 | GH_H2 | GH_H3 | GH_H5 | GH_H6)
+                           : (DRIFT_FIRST ? GH_G3 : (GH_G3 | GH_H1 | GH_H2));
+  GH gh = gh_functions<NEED>(gamma, beta0, sqb);
+  double g3bs = gh.g3;
+  double h1 = 0.0, h2 = 0.0;
+  double r = r0 * g0bs + eta * g1bs + k * g2bs;
+  double rinv = 1.0 / r;
+  double dfdt = (-k) * g1bs * rinv * r0inv;
+  double fm1, gmh, dgdtm1;
+  if (DRIFT_FIRST) {
+    fm1 = (-k) * r0inv * g2bs;
+    gmh = k * r0inv * (h * g2bs - r0 * g3bs);
+    dgdtm1 = k * r0inv * rinv * (h * g1bs - r0 * g2bs);
+  } else {
+    h1 = gh.h1;
+    h2 = gh.h2;
+    fm1 = k * rinv * (g2bs - k * r0inv * h1);
+    gmh = k * rinv * (r0 * h2 + eta * h1);
+    dgdtm1 = (-k) * rinv * g2bs;
+  }
+  for (int j = 0; j < 3; j++) delxv[j] = fm1 * x0[j] + gmh * v0[j];
+  for (int j = 0; j < 3; j++) delxv[3 + j] = dfdt * x0[j] + dgdtm1 * v0[j];
+  P.gamma = gamma; P.g0 = g0bs; P.g1 = g1bs; P.g2 = g2bs; P.g3 = g3bs; P.h1 = h1; P.h2 = h2;
+  P.dfdt = dfdt; P.fm1 = fm1; P.gmh = gmh; P.dgdtm1 = dgdtm1; P.r0 = r0; P.r = r; P.r0inv = r0inv; P.rinv = rinv;
+  P.k = k; P.h = h; P.beta = beta0; P.betainv = beta0inv; P.eta = eta; P.sqb = sqb; P.zeta = zeta;
+  P.H1v = gh.h1; P.H2v = gh.h2; P.H3v = gh.h3; P.H5v = gh.h5; P.H6v = gh.h6;
+}
+
+// compute_jacobian_gamma! (ahl21.jl:896-1139, debug = false).  jk is the 6x8
+// jac_kepler (col-major: jk[row + 6 col]); jm the 6-vector jac_mass.
+template <bool DRIFT_FIRST>
+__device__ __noinline__ void kep_jacobian(const KepParams& P, const double* x0, const double* v0, double* jk,
+                                             double* jm) {
+  const double G = GNEWT;
+  const double gamma = P.gamma, g0 = P.g0, g1 = P.g1, g2 = P.g2, g3 = P.g3, h1 = P.h1;
+  const double dfdt = P.dfdt, fm1 = P.fm1, gmh = P.gmh, dgdtm1 = P.dgdtm1, r0 = P.r0, r = P.r;
+  const double r0inv = P.r0inv, rinv = P.rinv, k = P.k, h = P.h, beta = P.beta, betainv = P.betainv;
+  const double eta = P.eta, sqb = P.sqb, zeta = P.zeta;
+  double r0inv2 = r0inv * r0inv;
+  double r0inv3 = r0inv2 * r0inv;
+  double rinv2 = rinv * rinv;
+  double rinv3 = rinv2 * rinv;
+  double hsq = h * h;
+  double ksq = k * k;
+  double d = (h + eta * g2 + 2.0 * k * g3) * betainv;
+  double c1 = d - r0 * g3;
+  double c2 = eta * g0 + g1 * zeta;
+  double c3 = d * k + g1 * (r0 * r0);
+  double h6 = P.H6v, h3 = P.H3v, h5 = P.H5v;
+  double h8 = (-(2.0 * h3)) + 3.0 * h5;
+  double dfm1dxx, dfm1dxv, dfm1dvx, dfm1dvv, dfm1dh, dfm1dk, dfm1dk2;
+  double dgmhdxx, dgmhdxv, dgmhdvx, dgmhdvv, dgmhdh, dgmhdk, dgmhdk2;
+  double ddfdtdxx, ddfdtdxv, ddfdtdvx, ddfdtdvv, ddfdtdk, ddfdtdk2, ddfdtdh;
+  double dgdxx, dgdxv, dgdvx, dgdvv, dgdk, dgdk2, dgdh;
+  if (DRIFT_FIRST) {
+    double c13 = g1 * h - g2 * r0;
+    double c9 = 2.0 * g2 * h - 3.0 * g3 * r0;
+    double c10 = k * (r0inv2 * r0inv2) * ((-g2) * r0 * h + k * c9 * betainv - c3 * c13 * rinv);
+    double c24 = r0inv3 * (r0 * (2.0 * k * r0inv - beta) * betainv - g1 * c3 * rinv / g2);
+    dfm1dxx = fm1 * c24;
+    dfm1dxv = (-fm1) * (g1 * rinv + h * c24);
+    dfm1dvx = dfm1dxv;
+    dfm1dvv = fm1 * rinv * ((-r0) * g2 + k * h6 * betainv / g2 + h * (2.0 * g1 + h * r * c24));
+    dfm1dh = fm1 * (g1 * rinv * (1.0 / g2 + 2.0 * k * r0inv - beta) - eta * c24);
+    dfm1dk = fm1 * (1.0 / k + g1 * c1 * rinv * r0inv / g2 - 2.0 * betainv * r0inv);
+    double h4 = (-P.H1v) * beta;
+    dfm1dk2 = (r0 * h4 + k * h6);
+    dgmhdxx = c10;
+    dgmhdxv = (-g2) * k * c13 * rinv * r0inv - h * c10;
+    dgmhdvx = dgmhdxv;
+    dgmhdvv = 2.0 * g2 * h * k * c13 * rinv * r0inv + hsq * c10 +
+              k * betainv * rinv * r0inv * ((r0 * r0) * h8 - beta * h * r0 * (g2 * g2) + (h * k + eta * r0) * h6);
+    dgmhdh = g2 * k * r0inv + k * c13 * rinv * r0inv + g2 * k * (2.0 * k * r0inv - beta) * c13 * rinv * r0inv -
+             eta * c10;
+    dgmhdk = r0inv * (k * c1 * c13 * rinv * r0inv + g2 * h - g3 * r0 - k * c9 * betainv * r0inv);
+    dgmhdk2 = (h6 * g3 * ksq + eta * r0 * (h6 + g2 * h4) + (r0 * r0) * g0 * h5 + k * eta * g2 * h6 +
+               (g1 * h6 + g3 * h4) * k * r0);
+    double c12 = g0 * h - g1 * r0;
+    double c17 = r0 - r - g2 * k;
+    double c21 = (g2 * k - r0) * (beta * c3 - k * g1 * r) * betainv * rinv2 * r0inv3 / g1 +
+                 eta * g1 * rinv * r0inv2 - 2.0 * r0inv2;
+    double c22 = rinv * ((-g1) - g0 * g2 / g1 + g2 * c2 * rinv);
+    double c25 = k * rinv * r0inv2 *
+                 ((-g2) + k * (c13 - g2 * r0) * betainv * r0inv2 - c13 * r0inv - c12 * c3 * rinv * r0inv2 +
+                  c13 * c2 * c3 * rinv2 * r0inv2 - c13 * (k * (g2 * k + r) - g0 * r0 * zeta) * betainv * rinv * r0inv2);
+    double c26 = k * rinv2 * r0inv * ((-g2) * c12 - g1 * c13 + g2 * c13 * c2 * rinv);
+    ddfdtdxx = dfdt * c21;
+    ddfdtdxv = dfdt * (c22 - h * c21);
+    ddfdtdvx = ddfdtdxv;
+    double c34 = ((-beta) * (eta * eta) * (g2 * g2) - eta * k * h8 - h6 * ksq - 2.0 * beta * eta * r0 * g1 * g2 +
+                  ((g2 * g2) - 3.0 * g1 * g3) * beta * k * r0 - beta * (g1 * g1) * (r0 * r0)) *
+                     betainv * rinv2 +
+                 (eta * (g2 * g2)) * rinv / g1 + (k * h8) * betainv * rinv / g1;
+    ddfdtdvv = dfdt * (c34 - 2.0 * h * c22 + hsq * c21);
+    ddfdtdk = dfdt * (1.0 / k - betainv * r0inv - c17 * betainv * rinv * r0inv -
+                      c1 * (g1 * c2 - g0 * r) * rinv2 * r0inv / g1);
+    ddfdtdk2 = (-(g2 * k - r0)) * (beta * r0 * (g3 - g1 * g2) - beta * eta * (g2 * g2) + k * h3) * betainv * rinv2 *
+               r0inv;
+    ddfdtdh = dfdt * (g0 * rinv / g1 - c2 * rinv2 - (2.0 * k * r0inv - beta) * c22 - eta * c21);
+    dgdxx = c25;
+    dgdxv = c26 - h * c25;
+    dgdvx = c26 - h * c25;
+    double h2 = P.H2v;
+    double c33 = d * k * rinv3 * r0inv * k * (h * g2 - r0 * g3) +
+                 k *
+                     ((-eta) * k * g1 * (g2 * g2) - g1 * g2 * g3 * ksq - r0 * eta * beta * g1 * (g2 * g2) -
+                      r0 * k * g1 * h2 - beta * (g2 * g2) * g0 * (r0 * r0)) *
+                     betainv * rinv2 * r0inv;
+    dgdvv = c33 - 2.0 * h * c26 + hsq * c25;
+    dgdk = rinv * r0inv *
+           ((-k) * (c13 - g2 * r0) * betainv * r0inv + c13 - k * c13 * c17 * betainv * rinv * r0inv +
+            k * c1 * c12 * rinv * r0inv - k * c1 * c2 * c13 * rinv2 * r0inv);
+    dgdk2 = k * betainv * rinv2 * r0inv *
+            ((-beta) * (eta * eta) * pow4(g2) + eta * g2 * (g1 * (g2 * g2) + (g1 * g1) * g3 - 5.0 * g2 * g3) * k +
+             g2 * g3 * h3 * ksq + 2.0 * eta * r0 * beta * (g2 * g2) * (g3 - g1 * g2) +
+             (4.0 * g3 - g0 * g3 - g1 * g2) * (g3 - g1 * g2) * r0 * k +
+             beta * (2.0 * g1 * g3 * g2 - (g1 * g1) * (g2 * g2) - (g3 * g3)) * (r0 * r0));
+    dgdh = g1 * k * rinv * r0inv + k * c12 * rinv2 * r0inv - k * c2 * c13 * rinv3 * r0inv -
+           (2.0 * k * r0inv - beta) * c26 - eta * c25;
+  } else {
+    const double h2 = P.h2;
+    double c14 = r0 * g2 - k * h1;
+    double c15 = eta * h1 + h2 * r0;
+    double c16 = eta * h2 + g1 * gamma * r0 / sqb;
+    double c17 = r0 - r - g2 * k;
+    double c19 = 4.0 * eta * h1 + 3.0 * h2 * r0;
+    double c23 = h2 * k - r0 * g1;
+    dfm1dxx = k * rinv3 * betainv * pow4(r0inv) *
+              (k * h1 * (r * r) * r0 * (beta - 2.0 * k * r0inv) + beta * c3 * (r * c23 + c14 * c2) +
+               c14 * r * (k * (r - g2 * k) + g0 * r0 * zeta));
+    dfm1dxv = k * rinv2 * r0inv * (k * (g2 * h2 + g1 * h1) - 2.0 * g1 * g2 * r0 + g2 * c14 * c2 * rinv);
+    dfm1dvx = dfm1dxv;
+    dfm1dvv = k * r0inv * rinv2 * betainv *
+              (2.0 * eta * k * (g2 * g3 - g1 * h1) + (3.0 * g3 * h2 - 4.0 * h1 * g2) * ksq +
+               beta * g2 * r0 * (3.0 * h1 * k - g2 * r0) +
+               c14 * rinv *
+                   ((-beta) * (g2 * g2) * (eta * eta) + eta * k * (2.0 * g0 * g3 - h2) - h6 * ksq +
+                    ((-(2.0 * eta)) * g1 * g2 + k * (h1 - 2.0 * g1 * g3)) * beta * r0 - beta * (g1 * g1) * (r0 * r0)));
+    dfm1dh = (g1 * k - h2 * ksq * r0inv - k * c14 * c2 * rinv * r0inv) * rinv2;
+    dfm1dk = rinv * r0inv *
+             (4.0 * h1 * ksq * betainv * r0inv - k * h1 - 2.0 * g2 * k * betainv + c14 -
+              k * c14 * c17 * betainv * rinv * r0inv + k * (g1 * r0 - k * h2) * c1 * rinv * r0inv -
+              k * c14 * c1 * c2 * rinv2 * r0inv);
+    dfm1dk2 = betainv * r0inv * rinv2 *
+              (r * (2.0 * eta * k * (g1 * h1 - g3 * g2) + (4.0 * g2 * h1 - 3.0 * g3 * h2) * ksq -
+                    eta * r0 * beta * g1 * h1 + (g3 * h2 - 4.0 * g2 * h1) * beta * k * r0 +
+                    g2 * h1 * (beta * beta) * (r0 * r0)) -
+               c14 * ((-(eta * eta)) * beta * (g2 * g2) - k * eta * h8 - ksq * h6 -
+                      eta * r0 * beta * (g1 * g2 + g0 * g3) + 2.0 * (h1 - g1 * g3) * beta * k * r0 -
+                      (g2 - beta * g1 * g3) * beta * (r0 * r0)));
+    dgmhdxx = k * rinv * r0inv *
+              (h2 + k * c19 * betainv * r0inv2 - c16 * c3 * rinv * r0inv2 +
+               c2 * c3 * c15 * ((rinv * r0inv) * (rinv * r0inv)) -
+               c15 * (k * (g2 * k + r) - g0 * r0 * zeta) * betainv * rinv * r0inv2);
+    dgmhdxv = k * rinv2 * (h1 * r - g2 * c16 - g1 * c15 + g2 * c2 * c15 * rinv);
+    dgmhdvx = dgmhdxv;
+    dgmhdvv = k * betainv * rinv2 *
+              (2.0 * (eta * eta) * (g1 * h1 - g2 * g3) + eta * k * (4.0 * g2 * h1 - 3.0 * h2 * g3) +
+               r0 * eta * (4.0 * g0 * h1 - 2.0 * g1 * g3) + 3.0 * r0 * k * ((g1 + beta * g3) * h1 - g3 * g2) +
+               (g0 * h8 - beta * g1 * ((g2 * g2) + g1 * g3)) * (r0 * r0) -
+               c15 * rinv *
+                   (beta * (g2 * g2) * (eta * eta) + eta * k * h8 + h6 * ksq +
+                    (2.0 * eta * g1 * g2 - k * ((g2 * g2) - 3.0 * g1 * g3)) * beta * r0 + beta * (g1 * g1) * (r0 * r0)));
+    dgmhdk = rinv * (k * c1 * c16 * rinv * r0inv + c15 - k * c15 * c17 * betainv * rinv * r0inv -
+                     k * c19 * betainv * r0inv - k * c1 * c2 * c15 * rinv2 * r0inv);
+    double h7 = beta * g1 * (g2 * g2) - g0 * h8;
+    dgmhdk2 = betainv * rinv2 *
+              (r * (2.0 * (eta * eta) * (g3 * g2 - g1 * h1) + eta * k * (3.0 * g3 * h2 - 4.0 * g2 * h1) +
+                    r0 * eta * (beta * g3 * (g1 * g2 + g0 * g3) - 2.0 * g0 * h6) +
+                    ((-h6) * (g1 + beta * g3) + g2 * (2.0 * g3 - h2)) * r0 * k +
+                    (h7 - (beta * beta) * g1 * (g3 * g3)) * (r0 * r0)) -
+               c15 * ((-beta) * (eta * eta) * (g2 * g2) + eta * k * ((-h2) + 2.0 * g0 * g3) - h6 * ksq -
+                      r0 * eta * beta * (h2 + 2.0 * g0 * g3) + 2.0 * beta * (2.0 * h1 - (g2 * g2)) * r0 * k +
+                      beta * (beta * g1 * g3 - g2) * (r0 * r0)));
+    dgmhdh = k * rinv3 * (r * c16 - c2 * c15);
+    ddfdtdxx = dfdt *
+               (eta * g1 * rinv - 2.0 - g0 * c3 * rinv * r0inv / g1 + c2 * c3 * r0inv * rinv2 -
+                k * (k * g2 - r0) * betainv * rinv * r0inv) *
+               r0inv2;
+    ddfdtdxv = (-dfdt) * (g0 * g2 / g1 + (r0 * g1 + eta * g2) * rinv) * rinv;
+    ddfdtdvx = ddfdtdxv;
+    ddfdtdvv = (-k) * rinv3 * r0inv * betainv *
+               ((beta * eta * (g2 * g2) + k * h8) * (r0 * g0 + k * g2) +
+                g1 * ((-h6) * ksq + ((-(2.0 * eta)) * g1 * g2 + (h1 - 2.0 * g1 * g3) * k) * beta * r0 -
+                      beta * (g1 * g1) * (r0 * r0)));
+    ddfdtdk = dfdt * (1.0 / k + c1 * (r0 - g2 * k) * r0inv * rinv2 / g1 - betainv * r0inv * (1.0 + c17 * rinv));
+    ddfdtdk2 = (r0 - g2 * k) * betainv * r0inv * rinv2 * ((-eta) * beta * (g2 * g2) + h3 * k + (g3 - g1 * g2) * beta * r0);
+    ddfdtdh = dfdt * (r0 - g2 * k) * rinv2 / g1;
+    dgdxx = rinv2 * r0inv3 *
+            ((eta * g2 + g1 * r0) * k * c3 * rinv + g2 * k * (k * (g2 * k - r) - g0 * r0 * zeta) * betainv);
+    dgdxv = k * g2 * rinv3 * (r * g1 + r0 * g1 + eta * g2);
+    dgdvx = dgdxv;
+    dgdvv = k * betainv * rinv3 *
+            ((eta * eta) * beta * (g2 * g2 * g2) - eta * k * g2 * h3 + 3.0 * r0 * eta * beta * g1 * (g2 * g2) +
+             r0 * k * ((-g0) * h6 + 3.0 * beta * g1 * g2 * g3) + beta * g2 * (g0 * g2 + (g1 * g1)) * (r0 * r0));
+    dgdk = rinv * r0inv *
+           ((-r0) * g2 + g2 * k * (r + r0 - g2 * k) * betainv * rinv - k * g1 * c1 * rinv + k * g2 * c1 * c2 * rinv2);
+    dgdk2 = betainv * rinv2 *
+            ((-beta) * (eta * eta) * (g2 * g2 * g2) + eta * k * g2 * h3 + eta * r0 * beta * g2 * (g3 - 2.0 * g1 * g2) +
+             (h6 - beta * (g2 * g2 * g2)) * r0 * k + beta * g1 * (g3 - g1 * g2) * (r0 * r0));
+    dgdh = k * rinv3 * (g2 * c2 - r * g1);
+  }
+  for (int q = 0; q < 48; q++) jk[q] = 0.0;
+  for (int j = 0; j < 3; j++) {
+    jk[j + 6 * j] = fm1;
+    jk[j + 6 * (3 + j)] = gmh;
+    for (int i = 0; i < 3; i++) {
+      jk[j + 6 * i] = jk[j + 6 * i] + ((dfm1dxx * x0[i] + dfm1dxv * v0[i]) * x0[j] +
+                                       (dgmhdxx * x0[i] + dgmhdxv * v0[i]) * v0[j]);
+      jk[j + 6 * (3 + i)] = jk[j + 6 * (3 + i)] + ((dfm1dvx * x0[i] + dfm1dvv * v0[i]) * x0[j] +
+                                                   (dgmhdvx * x0[i] + dgmhdvv * v0[i]) * v0[j]);
+    }
+    jk[j + 6 * 6] = dfm1dk * x0[j] + dgmhdk * v0[j];
+    jk[j + 6 * 7] = dfm1dh * x0[j] + dgmhdh * v0[j];
+    if (DRIFT_FIRST)
+      jm[j] = (G * r0inv) * (G * r0inv) * betainv * rinv * (dfm1dk2 * x0[j] - dgmhdk2 * v0[j]);
+    else
+      jm[j] = G * G * rinv * r0inv * (dfm1dk2 * x0[j] + dgmhdk2 * v0[j]);
+  }
+  for (int j = 0; j < 3; j++) {
+    jk[3 + j + 6 * j] = dfdt;
+    jk[3 + j + 6 * (3 + j)] = dgdtm1;
+    for (int i = 0; i < 3; i++) {
+      jk[3 + j + 6 * i] = jk[3 + j + 6 * i] + ((ddfdtdxx * x0[i] + ddfdtdxv * v0[i]) * x0[j] +
+                                               (dgdxx * x0[i] + dgdxv * v0[i]) * v0[j]);
+      jk[3 + j + 6 * (3 + i)] = jk[3 + j + 6 * (3 + i)] + ((ddfdtdvx * x0[i] + ddfdtdvv * v0[i]) * x0[j] +
+                                                           (dgdvx * x0[i] + dgdvv * v0[i]) * v0[j]);
+    }
+    jk[3 + j + 6 * 6] = ddfdtdk * x0[j] + dgdk * v0[j];
+    jk[3 + j + 6 * 7] = ddfdtdh * x0[j] + dgdh * v0[j];
+    if (DRIFT_FIRST)
+      jm[3 + j] = G * G * r0inv * rinv * (ddfdtdk2 * x0[j] + dgdk2 * v0[j]);
+    else
+      jm[3 + j] = G * G * rinv * r0inv * (ddfdtdk2 * x0[j] + dgdk2 * v0[j]);
+  }
+}
+
+}  // namespace nbg

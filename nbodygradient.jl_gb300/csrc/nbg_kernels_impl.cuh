@@ -1,0 +1,240 @@
+// nbg_kernels_impl.cuh -- the per-body-count kernels of libnbg_cuda and their
+// launchers.  Included only by nbg_inst.cu, which instantiates them for one
+// body count N per translation unit (the units compile in parallel).
+//
+// Work decomposition (one launch pair per chunk of K steps):
+//   orbit_chunk_kernel<N>     one lane per system: x, v, dq/dt, transit search
+//                             (src/transits/timing.jl:3-109); writes the step
+//                             operator records, tt and per-transit adjoint rows
+//   jacobian_chunk_kernel<N>  one lane per (system, column of jac_step): applies
+//                             the records with Kahan summation and turns each
+//                             transit's adjoint row into dtdq0 entries
+// Systems are grouped by (N, grad, kick pattern) so that every warp runs one
+// control-flow path; within a group systems are sorted longest first.
+#pragma once
+#include "../../include/nbg.h"
+#include "nbg_jacobian.cuh"
+
+namespace nbg {
+
+// Orbit producer for one chunk of K steps of one group (one lane per system).
+template <int N>
+__global__ void __launch_bounds__(PROD_BS) orbit_chunk_kernel(GroupArgs g, int chunk) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= g.S || g.sysidx[s] < 0) return;
+  const int S = g.S;
+  const long long nst = g.nsteps[s];
+  const long long k0 = (long long)chunk * g.K;
+  if (k0 >= nst) return;
+  Sys<N> st;
+  Work<N> w;
+  for (int q = 0; q < 3 * N; q++) {
+    st.x[q] = g.x[q * S + s];
+    st.v[q] = g.v[q * S + s];
+    st.xe[q] = g.xe[q * S + s];
+    st.ve[q] = g.ve[q * S + s];
+  }
+  for (int q = 0; q < N; q++) st.m[q] = g.m[q * S + s];
+  for (int q = 0; q < 7 * N; q++) st.dqdt[q] = g.dqdt[q * S + s];
+  double gsave[N];
+  long long count[N];
+  for (int q = 0; q < N; q++) {
+    gsave[q] = g.gsave[q * S + s];
+    count[q] = g.count[q * S + s];
+  }
+  const double t0 = g.t0[s], h = g.h[s], hI = g.hI[s];
+  const int ntt = g.ntt[s], ti = g.ti[s];
+  const uint64_t kick = g.kick;
+  const int gsys = g.sysidx[s];
+  unsigned int status = g.status[s];
+  for (int kk = 0; kk < g.K; kk++) {
+    const long long istep = k0 + kk;
+    if (istep >= nst) break;
+    if (g.grad) {
+      Rec rec{g.steprec + (size_t)kk * g.R * S + s, S};
+      if (istep == nst - 1) ahl21_step<N, true, true>(st, w, h, kick, rec);
+      else ahl21_step<N, true, false>(st, w, h, kick, rec);
+    } else {
+      ahl21_step<N, false, false>(st, w, h, kick, Rec{nullptr, 0});
+    }
+    const double t = t0 + (double)(istep + 1) * h;
+    // detect_transits! (timing.jl:3-28); the state after detection is the
+    // state before it (set_state!(s, s_prior)), so the search works on copies.
+    for (int o = 0; o < N - 1; o++) {
+      const int ib = (o < ti) ? o : o + 1;
+      const double gi = gsky(st, ib, ti);
+      const double xi = st.x[3 * ib], yi = st.x[3 * ib + 1], zi = st.x[3 * ib + 2];
+      const double ri = sqrt(xi * xi + yi * yi + zi * zi);
+      int flag = -1;
+      if (gi > 0.0 && gsave[ib] < 0.0 && -zi > 0.25 * ri && ri < 1e12) {
+        count[ib] += 1;
+        if (count[ib] <= ntt) {
+          // findtransit! (timing.jl:31-109)
+          double dt0 = -gi * hI / (gi - gsave[ib]);
+          double stmp = 0.0, tt1 = dt0 + 1.0, tt2 = dt0 + 2.0;
+          int iter = 0;
+          Sys<N> wk;
+          while (true) {
+            tt2 = tt1;
+            tt1 = dt0;
+            wk = st;
+            ahl21_step<N, true, true>(wk, w, dt0, kick, Rec{nullptr, 0});
+            const double gs = gsky(wk, ti, ib);
+            const double gd = gdot(wk, ti, ib);
+            const double dt = -gs / gd;
+            kahan(dt0, stmp, dt);
+            iter += 1;
+            if (iter >= 20 || dt0 == tt1 || dt0 == tt2) break;
+          }
+          if (iter >= 20) status |= NBG_STATUS_NEWTON_ITMAX;
+          const long long c = count[ib] - 1;
+          if (g.grad) {
+            wk = st;
+            Rec rec{g.scratch + s, S};
+            ahl21_step<N, true, true>(wk, w, dt0, kick, rec);
+            // dtbvdq! row 1 (timing.jl:155-171) as u^T jac_step with
+            // u^T = w^T S(dt0): w holds dg/dq at the transit, S the partial
+            // step's map on jac_step.  The consumer forms u^T J per column.
+            double u[7 * N];
+            for (int q = 0; q < 7 * N; q++) u[q] = 0.0;
+            const double dvx = wk.v[3 * ib] - wk.v[3 * ti], dvy = wk.v[3 * ib + 1] - wk.v[3 * ti + 1];
+            const double dx = wk.x[3 * ib] - wk.x[3 * ti], dy = wk.x[3 * ib + 1] - wk.x[3 * ti + 1];
+            u[7 * ib + 0] = dvx;
+            u[7 * ti + 0] = -dvx;
+            u[7 * ib + 1] = dvy;
+            u[7 * ti + 1] = -dvy;
+            u[7 * ib + 3] = dx;
+            u[7 * ti + 3] = -dx;
+            u[7 * ib + 4] = dy;
+            u[7 * ti + 4] = -dy;
+            adjoint_step<N>(u, dt0, kick, rec);
+            const double gd = gdot(wk, ti, ib);
+            double* tr = g.trec + ((size_t)(kk * (N - 1) + o) * (7 * N + 1)) * S + s;
+            for (int q = 0; q < 7 * N; q++) tr[(size_t)q * S] = u[q];
+            tr[(size_t)(7 * N) * S] = gd;
+            flag = (int)c;
+          }
+          g.tt[g.off_tt[gsys] + ib + (long long)N * c] = t + dt0;
+        } else {
+          status |= NBG_STATUS_NTT_OVERFLOW;
+        }
+      }
+      if (g.grad) g.tflag[(size_t)(kk * (N - 1) + o) * S + s] = flag;
+      gsave[ib] = gi;
+    }
+  }
+  for (int q = 0; q < 3 * N; q++) {
+    g.x[q * S + s] = st.x[q];
+    g.v[q * S + s] = st.v[q];
+    g.xe[q * S + s] = st.xe[q];
+    g.ve[q * S + s] = st.ve[q];
+  }
+  if (g.grad && nst <= k0 + g.K)  // the chunk that ran the last step holds the final dq/dt
+    for (int q = 0; q < 7 * N; q++) g.dqdt[q * S + s] = st.dqdt[q];
+  for (int q = 0; q < N; q++) {
+    g.gsave[q * S + s] = gsave[q];
+    g.count[q * S + s] = count[q];
+  }
+  g.status[s] = status;
+}
+
+// Jacobian consumer for one chunk of K steps (one lane per column).
+template <int N>
+__global__ void __launch_bounds__(CONS_BS) jacobian_chunk_kernel(GroupArgs g, int chunk) {
+  extern __shared__ double smem[];
+  constexpr int M = 7 * N, R6 = 6 * N;
+  const int f = blockIdx.x * CONS_BS + threadIdx.x;
+  const int s = f / M, c = f % M;
+  if (s >= g.S || g.sysidx[s] < 0) return;
+  const int S = g.S;
+  const long long nst = g.nsteps[s];
+  const long long k0 = (long long)chunk * g.K;
+  if (k0 >= nst) return;
+  double* J = smem + threadIdx.x;
+  double* E = smem + R6 * CONS_BS + threadIdx.x;
+  const double* Jg = g.Jint + (size_t)s * R6 * M + c;
+  const double* Eg = g.Eint + (size_t)s * R6 * M + c;
+  for (int r = 0; r < R6; r++) {
+    J[r * CONS_BS] = Jg[(size_t)r * M];
+    E[r * CONS_BS] = Eg[(size_t)r * M];
+  }
+  const double h = g.h[s];
+  const int ntt = g.ntt[s], ti = g.ti[s];
+  const int gsys = g.sysidx[s];
+  const uint64_t kick = g.kick;
+  const int cb = c / 7, ck = c % 7;  // column c is d/d q0[ck] of body cb
+  for (int kk = 0; kk < g.K; kk++) {
+    const long long istep = k0 + kk;
+    if (istep >= nst) break;
+    Rec rec{g.steprec + (size_t)kk * g.R * S + s, S};
+    apply_step<N, CONS_BS>(J, E, c, h, kick, rec);
+    for (int o = 0; o < N - 1; o++) {
+      const int flag = g.tflag[(size_t)(kk * (N - 1) + o) * S + s];
+      if (flag < 0) continue;
+      const double* tr = g.trec + ((size_t)(kk * (N - 1) + o) * (7 * N + 1)) * S + s;
+      double acc = 0.0;
+      for (int b = 0; b < N; b++)
+        for (int r = 0; r < 6; r++) {
+          const double ur = tr[(size_t)(7 * b + r) * S];
+          acc = fma(ur, J[(6 * b + r) * CONS_BS], acc);
+          acc = fma(ur, E[(6 * b + r) * CONS_BS], acc);
+        }
+      if (ck == 6) acc = acc + tr[(size_t)c * S];  // unit mass row of this column
+      const double gd = tr[(size_t)(7 * N) * S];
+      const int ib = (o < ti) ? o : o + 1;
+      g.dtdq0[g.off_dq[gsys] + ib + (long long)N * (flag + (long long)ntt * (ck + 7LL * cb))] = -acc / gd;
+    }
+  }
+  double* Jw = g.Jint + (size_t)s * R6 * M + c;
+  double* Ew = g.Eint + (size_t)s * R6 * M + c;
+  for (int r = 0; r < R6; r++) {
+    Jw[(size_t)r * M] = J[r * CONS_BS];
+    Ew[(size_t)r * M] = E[r * CONS_BS];
+  }
+}
+
+// gsave[i] = g!(i, ti, x, v) for every occultor (Transits.jl:146-149).
+template <int N>
+__global__ void seed_gsave_kernel(GroupArgs g) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= g.S || g.sysidx[s] < 0) return;
+  const int S = g.S, ti = g.ti[s];
+  for (int i = 0; i < N; i++) {
+    if (i == ti) continue;
+    const double dx = g.x[(3 * ti) * S + s] - g.x[(3 * i) * S + s];
+    const double dy = g.x[(3 * ti + 1) * S + s] - g.x[(3 * i + 1) * S + s];
+    const double dvx = g.v[(3 * ti) * S + s] - g.v[(3 * i) * S + s];
+    const double dvy = g.v[(3 * ti + 1) * S + s] - g.v[(3 * i + 1) * S + s];
+    g.gsave[i * S + s] = dx * dvx + dy * dvy;
+  }
+}
+
+template <int N>
+int launch_orbit(const GroupArgs& g, int chunk, cudaStream_t st) {
+  int blocks = (g.S + PROD_BS - 1) / PROD_BS;
+  orbit_chunk_kernel<N><<<blocks, PROD_BS, 0, st>>>(g, chunk);
+  return 0;
+}
+
+template <int N>
+int launch_jac(const GroupArgs& g, int chunk, cudaStream_t st) {
+  long long threads = (long long)g.S * 7 * N;
+  int blocks = (int)((threads + CONS_BS - 1) / CONS_BS);
+  size_t smem = (size_t)2 * 6 * N * CONS_BS * sizeof(double);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(jacobian_chunk_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr_set = true;
+  }
+  jacobian_chunk_kernel<N><<<blocks, CONS_BS, smem, st>>>(g, chunk);
+  return 0;
+}
+
+template <int N>
+int launch_seed(const GroupArgs& g, cudaStream_t st) {
+  int b = (g.S + 127) / 128;
+  seed_gsave_kernel<N><<<b, 128, 0, st>>>(g);
+  return 0;
+}
+
+}  // namespace nbg

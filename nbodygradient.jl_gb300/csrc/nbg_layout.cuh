@@ -1,0 +1,55 @@
+// nbg_layout.cuh -- data layout shared by the host orchestration and the
+// kernels of libnbg_cuda: operator-record sizes, the per-group argument block
+// and the launcher declarations (definitions live in nbg_kernels_impl.cuh and
+// are instantiated once per body count by nbg_inst.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nbg {
+
+// Pair record: K[36] (row-major r*6+l), mi, mj, jac_ij[:,m_i] (12), jac_ij[:,m_j] (12)
+constexpr int PREC = 62;
+constexpr int PREC_MI = 36, PREC_MJ = 37, PREC_MC6 = 38, PREC_MC13 = 50;
+
+__host__ __device__ constexpr int op_size(int N) { return 12 * N * N; }
+__host__ __device__ inline int pair_bit(int i, int j, int N) { return i * N - i * (i + 1) / 2 + (j - i - 1); }
+
+// Record size of one step for N bodies with npk Kepler pairs; kick operators
+// only when the group has kick pairs.
+__host__ __device__ inline int step_record_size(int N, int npk, bool kick) {
+  return (kick ? 2 * op_size(N) : 0) + 2 * npk * PREC + op_size(N);
+}
+
+constexpr int PROD_BS = 32;   // orbit producer: one warp per block, spread over SMs
+constexpr int CONS_BS = 128;  // Jacobian consumer: four warps per block
+
+struct GroupArgs {
+  int N, S, nsys, grad, K, R, npk;
+  unsigned long long kick;
+  // per-system state, structure of arrays: element e of system s at [e * S + s]
+  double *x, *v, *xe, *ve, *m, *dqdt, *gsave;
+  long long* count;  // [N][S]
+  double *t0, *h, *hI;
+  long long* nsteps;
+  int *ntt, *ti, *sysidx;
+  unsigned int* status;
+  // packed outputs in the caller's layout, indexed by global system
+  double* tt;
+  const long long* off_tt;
+  double* dtdq0;
+  const long long* off_dq;
+  // records
+  double* steprec;  // [K][R][S]
+  double* trec;     // [K][N-1][7N+1][S]
+  int* tflag;       // [K][N-1][S]
+  double* scratch;  // [R][S]
+  // consumer state: non-mass rows of jac_step / jac_error, [S][6N][7N]
+  double *Jint, *Eint;
+};
+
+template <int N> int launch_orbit(const GroupArgs& g, int chunk, cudaStream_t st);
+template <int N> int launch_jac(const GroupArgs& g, int chunk, cudaStream_t st);
+template <int N> int launch_seed(const GroupArgs& g, cudaStream_t st);
+
+}  // namespace nbg
