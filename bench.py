@@ -1,0 +1,389 @@
+#!/usr/bin/env python3
+"""Benchmark: batched AHL21 integration with Jacobian and transit timing (grad=true).
+
+Metric: system-steps/s, the number of AHL21 steps of all systems
+(sum over systems of round(tmax/h); transit-Newton sub-steps are not counted)
+divided by the time of one pass over the workload.  One bench "step" is one
+full integration of the whole synthetic batch: intr(s, tt; grad=true) for
+every system.
+
+Default workload (the configuration the metric is quoted on): batch_3body,
+4096 3-body systems, h = 0.5 d, tmax = 1000 d (2000 steps each).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Arms:
+  gb300      libnbg_cuda through its C ABI.  `value`: inputs already resident
+             in HBM (nbg_batch_integrate_transits_device); `e2e`: the host API
+             (nbg_batch_integrate_transits) on pinned host buffers with the
+             host<->device copies inside the timed region.
+  reference  the CPU restatement of the reference (oracle/, built from C++,
+             Julia is not available) on all host cores, on a bounded sample of
+             the same workload.
+
+Under torchrun each rank integrates its own replica of the workload on its
+own GPU (weak scaling, no collective on the data path); value is the sum of
+all ranks' system-steps over the maximum rank time.
+"""
+import argparse
+import ctypes
+import importlib.util
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(ROOT, "nbodygradient.jl_gb300")
+
+
+def load_package():
+    if "nbg" in sys.modules:
+        return sys.modules["nbg"]
+    spec = importlib.util.spec_from_file_location("nbg", os.path.join(PKG_DIR, "__init__.py"),
+                                                  submodule_search_locations=[PKG_DIR])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["nbg"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def flops_per_system_step(n):
+    """Algorithmic FP64 flops of the Jacobian consumer per system-step (FMA = 2).
+
+    Per column of jac_step and step: 2P pair updates of 132 flops (6 differences,
+    a 6x6 product u = K D (66), the two mass-ratio scalings (12) and the Kahan
+    sums of 12 rows (48)); the phi block 3N x 3N (18 N^2) with its Kahan sums
+    (12 N + 9 N); two kick folds (36 N); two drifts (30 N).  7N columns.
+    """
+    P = n * (n - 1) // 2
+    per_col = 2 * P * 132 + 18 * n * n + 87 * n
+    return per_col * 7 * n
+
+
+def build_workload(nbg, name, nsys=None, seed=0):
+    W = nbg.workloads
+    if name == "batch_3body":
+        els, h, tmax = W.batch_3body(nsys or 4096, seed)
+        hs, tms = [h] * len(els), [tmax] * len(els)
+    elif name == "batch_8body":
+        els, h, tmax = W.batch_8body(nsys or 1024, seed)
+        hs, tms = [h] * len(els), [tmax] * len(els)
+    elif name == "batch_uneven":
+        els, hs, tms = W.batch_uneven(nsys or 2048, seed)
+    elif name == "plain_3body":
+        el, h, tmax = W.plain_3body(seed)
+        els, hs, tms = [el], [h], [tmax]
+    else:
+        raise SystemExit("unknown workload %s" % name)
+    states, ics = [], []
+    for el in els:
+        ic = W.ic_of(el)
+        ics.append(ic)
+        states.append(nbg.State(ic))
+    # one transit-array shape per body count (the CPU baseline packs equal shapes)
+    ntt_n = {}
+    for ic, tmax in zip(ics, tms):
+        ntt_n[ic.nbody] = max(ntt_n.get(ic.nbody, 0), nbg.TransitTiming(tmax, ic).ntt)
+    timings = [nbg.TransitTiming(tmax, ic, ntt=ntt_n[ic.nbody]) for ic, tmax in zip(ics, tms)]
+    nsteps = [abs(int(np.rint(t / h))) for t, h in zip(tms, hs)]
+    return states, timings, hs, tms, nsteps
+
+
+def make_batch(nbg, states, timings, hs, tms, pinned=False):
+    b = nbg.Batch([s.n for s in states], [t.ti - 1 for t in timings], hs, tms, [t.ntt for t in timings], True)
+    if pinned:
+        import torch
+        for k, a in list(b.arrays.items()):
+            t = torch.empty(a.shape, dtype=getattr(torch, str(a.dtype)), pin_memory=True)
+            b.arrays[k] = t.numpy()
+            b.arrays[k][...] = 0
+            b.__dict__.setdefault("_pinned", []).append(t)
+    for q in range(len(states)):
+        b.set_system(q, states[q], timings[q])
+    return b
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle-reason sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) >= 9:
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(nbg, states, timings, hs, tms, nsteps, target_s=12.0, nthreads=None):
+    """The oracle (CPU restatement of the reference), batched over host threads, on a sample."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as O
+    O.build()
+    L = O.lib()
+    nthreads = nthreads or os.cpu_count() or 1
+    # calibrate on one system, then size the sample to ~target_s of wall time
+    total_ss, total_t, used = 0, 0.0, 0
+    sample = max(1, nthreads)
+    q = 0
+    while total_t < target_s and q < len(states):
+        idx = [(q + r) % len(states) for r in range(sample)]
+        q += sample
+        b = make_batch(nbg, [states[i] for i in idx], [timings[i] for i in idx], [hs[i] for i in idx],
+                       [tms[i] for i in idx])
+        a = b.arrays
+        p = O._p
+        n = int(b.n[0])
+        assert np.all(b.n == n) and np.all(b.ntt == b.ntt[0]), "the batched oracle needs equal shapes"
+        t0 = time.perf_counter()
+        rc = L.oracle_integrate_transits_batch(
+            len(idx), nthreads, n, int(b.ti[0]), p(b.h), p(b.tmax), 1, p(a["t"]), p(a["x"]), p(a["v"]), p(a["m"]),
+            p(a["xerror"]), p(a["verror"]), p(a["jac_step"]), p(a["jac_error"]), p(a["dqdt"]), p(a["pair"], O._U8),
+            p(a["jac_init"]), int(b.ntt[0]), p(a["tt"]), p(a["dtdq0"]), p(a["dtdelements"]), p(a["count"], O._I64))
+        dt = time.perf_counter() - t0
+        assert rc == 0
+        total_ss += sum(nsteps[i] for i in idx)
+        total_t += dt
+        used += len(idx)
+        if total_t < 1.0:
+            sample *= 4
+    return total_ss / total_t, nthreads, used, total_t
+
+
+def replica_seed(seed, rank):
+    """Each rank integrates its own draw of the workload (replicas, weak scaling)."""
+    return seed + 1000 * rank
+
+
+def reduce_max_ms(ms, dist):
+    """Maximum of the per-rank step times (the job is as slow as its slowest rank)."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0])
+
+
+def aggregate_value(system_steps_per_rank, world, ms):
+    """Whole-job system-steps/s: all ranks' work over the slowest rank's time."""
+    return system_steps_per_rank * world / (ms * 1e-3)
+
+
+def _same_n(states):
+    return len({s.n for s in states}) == 1
+
+
+def run_reference(args, nbg, rank):
+    """--impl reference: the oracle on the host cores, K timed bounded samples."""
+    if rank != 0:
+        return
+    states, timings, hs, tms, nsteps = build_workload(nbg, args.workload, args.nsys, args.seed)
+    if not _same_n(states):
+        states_i = [i for i, s in enumerate(states) if s.n == states[0].n]
+        states = [states[i] for i in states_i]
+        timings = [timings[i] for i in states_i]
+        hs = [hs[i] for i in states_i]
+        tms = [tms[i] for i in states_i]
+        nsteps = [nsteps[i] for i in states_i]
+    vals = []
+    for it in range(args.warmup + args.steps):
+        v, cores, used, t = cpu_baseline(nbg, states, timings, hs, tms, nsteps, target_s=args.ref_seconds)
+        if it >= args.warmup:
+            vals.append((v, used, t))
+    value = float(np.mean([v for v, _, _ in vals]))
+    used = vals[-1][1]
+    line = {
+        "impl": "reference", "metric": "system_steps_per_s", "value": value, "unit": "system-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": float(np.mean([t for _, _, t in vals])) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "nsys": len(states), "grad": True},
+        "cpu_baseline": {"value": value, "unit": "system-steps/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": "%d systems of %s per step (C++ restatement of the reference, "
+                                   "Julia unavailable)" % (used, args.workload)},
+        "e2e": {"value": value, "unit": "system-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="batch_3body",
+                    choices=["batch_3body", "batch_8body", "batch_uneven", "plain_3body"])
+    ap.add_argument("--nsys", type=int, default=None)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--chunk", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-seconds", type=float, default=8.0)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    nbg = load_package()
+    if args.impl == "reference":
+        run_reference(args, nbg, rank)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    import torch
+    torch.cuda.set_device(local_rank)
+    ctx = nbg.Context(local_rank)
+    if args.chunk:
+        ctx.set_tuning(chunk_steps=args.chunk)
+    states, timings, hs, tms, nsteps = build_workload(nbg, args.workload, args.nsys, replica_seed(args.seed, rank))
+    total_ss = int(sum(nsteps))
+    b = make_batch(nbg, states, timings, hs, tms)
+    # device-resident inputs: a pristine copy and the working buffers
+    dev0 = {k: torch.from_numpy(a.copy()).cuda() for k, a in b.arrays.items()}
+    dev = {k: torch.empty_like(t) for k, t in dev0.items()}
+
+    def reset():
+        for k in dev:
+            dev[k].copy_(dev0[k])
+
+    def step():
+        reset()
+        b.run_device(dev, ctx)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = ClockSampler(local_rank)
+    clk.start()
+    launches = 0
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+        launches += ctx.last_launch_count()
+    e1.record()
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = reduce_max_ms(e0.elapsed_time(e1) / args.steps, dist)
+    value = aggregate_value(total_ss, world, ms)
+
+    # e2e through the host API with pinned buffers, copies inside the timed region
+    bp = make_batch(nbg, states, timings, hs, tms, pinned=True)
+    pristine = {k: a.copy() for k, a in bp.arrays.items()}
+    in_keys = ("t", "x", "v", "m", "xerror", "verror", "jac_step", "jac_error", "dqdt", "jac_init", "count")
+    out_keys = ("t", "x", "v", "xerror", "verror", "jac_step", "jac_error", "dqdt", "count", "tt", "dtdq0",
+                "dtdelements")
+    h2d = sum(bp.arrays[k].nbytes for k in in_keys)
+    d2h = sum(bp.arrays[k].nbytes for k in out_keys)
+    e2e_ms = []
+    for it in range(1 + args.e2e_steps if args.e2e_steps > 0 else 0):
+        for k in bp.arrays:
+            bp.arrays[k][...] = pristine[k]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        bp.run(ctx)
+        torch.cuda.synchronize()
+        if it > 0:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_val = total_ss * world / (np.mean(e2e_ms) * 1e-3) if e2e_ms else None
+
+    # roofline of the dominant kernel (Jacobian consumer) from one profiled pass
+    ctx.set_profiling(True)
+    step()
+    ctx.set_profiling(False)
+    total_ms, orbit_ms, jac_ms = ctx.last_timing()
+    n_orbit, n_jac = ctx.last_kernel_stats()
+    flops = sum(flops_per_system_step(s.n) * ns for s, ns in zip(states, nsteps))
+    peak = ctx.fp64_peak_tflops()
+    achieved = flops / (jac_ms * 1e-3) / 1e12 if jac_ms > 0 else None
+    traffic = None
+    prof_json = os.path.join(ROOT, "profiles", "jacobian_consumer_%s.json" % args.workload)
+    if os.path.exists(prof_json):
+        with open(prof_json) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+
+    if rank == 0:
+        line = {
+            "metric": "system_steps_per_s", "value": value, "unit": "system-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded draws)",
+            "config": {"workload": args.workload, "nsys": len(states), "system_steps_per_pass": total_ss,
+                       "grad": True, "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "working set larger than L2 (operator records + jac_step)",
+                       "chunk_steps": args.chunk or 16},
+            "e2e": {"value": e2e_val, "unit": "system-steps/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.mean(e2e_ms)) if e2e_ms else None},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "kernel": "jacobian_chunk_kernel", "peak_source": "measured live (nbg_fp64_peak, DFMA)",
+                         "launches": n_jac, "kernel_ms": jac_ms, "orbit_ms": orbit_ms, "loop_ms": total_ms},
+            "clocks": clocks,
+        }
+        if not args.no_cpu_baseline and world == 1:
+            v, cores, used, t = cpu_baseline(nbg, states, timings, hs, tms, nsteps) if _same_n(states) else \
+                (None, None, 0, 0.0)
+            line["cpu_baseline"] = {"value": v, "unit": "system-steps/s", "cores": cores, "kind": "port",
+                                    "sample": "%d systems of %s, %.1f s on %s host threads" %
+                                              (used, args.workload, t, cores)}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

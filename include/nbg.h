@@ -120,8 +120,9 @@ int nbg_batch_integrate_transits(nbg_context* ctx, int nsys, const nbg_system_de
 
 /*
  * Same as nbg_batch_integrate_transits, but every array pointer (and desc)
- * is a DEVICE pointer of the context's device, already resident in HBM.
- * Used when the caller keeps systems on the GPU between calls.
+ * is a DEVICE pointer of the context's device, already resident in HBM
+ * (desc_host and status stay host pointers).  Used when the caller keeps
+ * systems on the GPU between calls.
  */
 int nbg_batch_integrate_transits_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc_host, double* t,
                                         double* x, double* v, const double* m, double* xerror, double* verror,
@@ -134,13 +135,25 @@ int nbg_batch_integrate_transits_device(nbg_context* ctx, int nsys, const nbg_sy
  * producer and the Jacobian consumer on two streams. */
 int nbg_set_tuning(nbg_context* ctx, int chunk_steps, int overlap);
 
-/* Device time (ms) of the last batched call's kernels, measured with CUDA
- * events on the context's stream: total, orbit-producer share, Jacobian
- * consumer share. */
+/* Device time (ms) of the last batched call's integration, measured with
+ * CUDA events on the context's stream: total (chunk loop), and -- when
+ * profiling is on -- the summed durations of the orbit-producer and
+ * Jacobian-consumer launches.  No counterpart in the reference. */
 int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double* jacobian_ms);
+
+/* Record an event pair around every orbit / Jacobian launch (off by default). */
+int nbg_set_profiling(nbg_context* ctx, int on);
+
+/* Launch counts of the last call, per kernel kind. */
+int nbg_last_kernel_stats(nbg_context* ctx, int64_t* orbit_launches, int64_t* jacobian_launches);
 
 /* Number of kernels launched by the last call. */
 int64_t nbg_last_launch_count(nbg_context* ctx);
+
+/* Measured FP64 FMA throughput of the context's device (TFLOP/s, FMA = 2
+ * flops): the roofline denominator for the FP64-bound kernels.  No
+ * counterpart in the reference; a measurement helper. */
+int nbg_fp64_peak(nbg_context* ctx, double* tflops);
 
 #ifdef __cplusplus
 }

@@ -20,7 +20,7 @@ import math
 
 import numpy as np
 
-from . import _lib
+from . import _lib, build, workloads
 from ._lib import Context, NbgError, SystemDesc, default_context, device_info
 from .ics import CartesianIC, Elements, ElementsIC, hierarchy_nested, init_nbody, kepler_init
 
@@ -80,13 +80,20 @@ def _ntt(tmax, periods):
 
 
 class TransitTiming:
-    """Transit times and derivatives (src/transits/Transits.jl:14-56).  ti is 1-based."""
+    """Transit times and derivatives (src/transits/Transits.jl:14-56).  ti is 1-based.
 
-    def __init__(self, tmax, ic, ti=1):
+    ntt defaults to the reference's max_i ceil(|tmax / P_i|) + 3; a larger
+    value may be given so that a batch of systems shares one output shape.
+    """
+
+    def __init__(self, tmax, ic, ti=1, ntt=None):
         n = ic.nbody
         if not (1 <= ti <= n):
             raise ValueError("ti must be in 1..%d" % n)
-        ntt = _ntt(tmax, ic.elements[:, 1])
+        ntt_ref = _ntt(tmax, ic.elements[:, 1])
+        if ntt is not None and ntt < ntt_ref:
+            raise ValueError("ntt = %d is below the reference's %d" % (ntt, ntt_ref))
+        ntt = ntt_ref if ntt is None else int(ntt)
         self.n, self.ntt, self.ti = n, ntt, ti
         self.tt = np.zeros((n, ntt), order="F")
         self.dtdq0 = np.zeros((n, ntt, 7, n), order="F")

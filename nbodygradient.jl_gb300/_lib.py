@@ -30,7 +30,8 @@ MAX_BODIES = 10
 EXPORTS = (
     "nbg_create", "nbg_destroy", "nbg_last_error", "nbg_version", "nbg_device_info",
     "nbg_integrate_transits", "nbg_batch_integrate_transits", "nbg_batch_integrate_transits_device",
-    "nbg_set_tuning", "nbg_last_timing", "nbg_last_launch_count",
+    "nbg_set_tuning", "nbg_last_timing", "nbg_last_launch_count", "nbg_fp64_peak",
+    "nbg_set_profiling", "nbg_last_kernel_stats",
 )
 
 
@@ -91,6 +92,9 @@ def load(build_if_missing=True):
     L.nbg_last_timing.argtypes = [_VP, _D, _D, _D]
     L.nbg_last_launch_count.argtypes = [_VP]
     L.nbg_last_launch_count.restype = ctypes.c_int64
+    L.nbg_fp64_peak.argtypes = [_VP, _D]
+    L.nbg_set_profiling.argtypes = [_VP, ctypes.c_int]
+    L.nbg_last_kernel_stats.argtypes = [_VP, _I64, _I64]
     _lib = L
     return L
 
@@ -150,6 +154,19 @@ class Context:
 
     def last_launch_count(self):
         return int(load().nbg_last_launch_count(self._h))
+
+    def set_profiling(self, on=True):
+        check(load().nbg_set_profiling(self._h, int(bool(on))))
+
+    def last_kernel_stats(self):
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        check(load().nbg_last_kernel_stats(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def fp64_peak_tflops(self):
+        v = ctypes.c_double()
+        check(load().nbg_fp64_peak(self._h, ctypes.byref(v)))
+        return v.value
 
 
 _default_ctx = None

@@ -180,8 +180,20 @@ struct nbg_context {
   int chunk_steps = 16;
   int overlap = 0;
   double last_total_ms = 0, last_orbit_ms = 0, last_jac_ms = 0;
-  long long last_launches = 0;
+  long long last_launches = 0, last_orbit_launches = 0, last_jac_launches = 0;
+  int profile = 0;
+  std::vector<cudaEvent_t> prof_events;  // pairs around each timed launch
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  int event(size_t i, cudaEvent_t* out) {
+    while (prof_events.size() <= i) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) return set_error(NBG_ECUDA, "cudaEventCreate failed");
+      prof_events.push_back(e);
+    }
+    *out = prof_events[i];
+    return NBG_OK;
+  }
 
   // Grow-only device buffer cache keyed by name.
   template <class T>
@@ -379,16 +391,34 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
   long long max_steps = 0;
   for (auto& kv : groups) max_steps = std::max(max_steps, kv.second.max_steps);
   const long long nchunks = (max_steps + K - 1) / K;
+  // profiling: an event pair around every orbit / Jacobian launch
+  std::vector<std::pair<int, size_t>> prof;  // (kind, first event index)
+  size_t nev = 0;
+  auto timed = [&](int kind, auto&& launch) -> int {
+    if (!ctx->profile) return launch();
+    cudaEvent_t a, b;
+    int r;
+    if ((r = ctx->event(nev, &a)) || (r = ctx->event(nev + 1, &b))) return r;
+    cudaEventRecord(a, st);
+    r = launch();
+    cudaEventRecord(b, st);
+    prof.emplace_back(kind, nev);
+    nev += 2;
+    return r;
+  };
+  ctx->last_orbit_launches = ctx->last_jac_launches = 0;
   NBG_CUDA(cudaEventRecord(ctx->ev0, st));
   for (long long c = 0; c < nchunks; c++) {
     for (size_t q = 0; q < gargs.size(); q++) {
       const GroupArgs& g = gargs[q];
       if (c * K >= gmaxsteps[q]) continue;
-      kOrbit[g.N](g, (int)c, st);
+      if ((rc = timed(0, [&] { return kOrbit[g.N](g, (int)c, st); }))) return rc;
       ctx->last_launches++;
+      ctx->last_orbit_launches++;
       if (g.grad) {
-        kJac[g.N](g, (int)c, st);
+        if ((rc = timed(1, [&] { return kJac[g.N](g, (int)c, st); }))) return rc;
         ctx->last_launches++;
+        ctx->last_jac_launches++;
       }
     }
   }
@@ -423,6 +453,11 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
   float ms = 0;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   ctx->last_total_ms = ms;
+  for (auto& pr : prof) {
+    float e = 0;
+    cudaEventElapsedTime(&e, ctx->prof_events[pr.second], ctx->prof_events[pr.second + 1]);
+    (pr.first ? ctx->last_jac_ms : ctx->last_orbit_ms) += e;
+  }
   if (status_host) {
     std::fill(status_host, status_host + nsys, 0u);
     for (auto& g : gargs) {
@@ -438,6 +473,25 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
 }
 
 }  // namespace
+
+// FP64 FMA throughput probe: CHAINS independent FMA chains per thread, full
+// warps, several blocks per SM.  Every index stays inside the grid-sized
+// output buffer.
+constexpr int PEAK_CHAINS = 8;
+__global__ void fp64_peak_kernel(double* out, int iters) {
+  double a[PEAK_CHAINS];
+  const double b = 1.0000001 + 1e-9 * threadIdx.x, c = 1e-7;
+#pragma unroll
+  for (int k = 0; k < PEAK_CHAINS; k++) a[k] = 1.0 + k * 1e-3;
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int k = 0; k < PEAK_CHAINS; k++) a[k] = fma(a[k], b, c);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < PEAK_CHAINS; k++) s += a[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
 
 // ===================================================================== C ABI
 
@@ -492,6 +546,7 @@ int nbg_destroy(nbg_context* ctx) {
     if (kv.second.p) cudaFree(kv.second.p);
   cudaEventDestroy(ctx->ev0);
   cudaEventDestroy(ctx->ev1);
+  for (auto e : ctx->prof_events) cudaEventDestroy(e);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return NBG_OK;
@@ -505,6 +560,19 @@ int nbg_set_tuning(nbg_context* ctx, int chunk_steps, int overlap) {
   return NBG_OK;
 }
 
+int nbg_set_profiling(nbg_context* ctx, int on) {
+  if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
+  ctx->profile = on ? 1 : 0;
+  return NBG_OK;
+}
+
+int nbg_last_kernel_stats(nbg_context* ctx, int64_t* orbit_launches, int64_t* jacobian_launches) {
+  if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
+  if (orbit_launches) *orbit_launches = ctx->last_orbit_launches;
+  if (jacobian_launches) *jacobian_launches = ctx->last_jac_launches;
+  return NBG_OK;
+}
+
 int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double* jacobian_ms) {
   if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
   if (total_ms) *total_ms = ctx->last_total_ms;
@@ -514,6 +582,31 @@ int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double
 }
 
 int64_t nbg_last_launch_count(nbg_context* ctx) { return ctx ? ctx->last_launches : -1; }
+
+int nbg_fp64_peak(nbg_context* ctx, double* tflops) {
+  if (!ctx || !tflops) return set_error(NBG_EINVAL, "NULL argument");
+  NBG_CUDA(cudaSetDevice(ctx->device));
+  cudaDeviceProp p;
+  NBG_CUDA(cudaGetDeviceProperties(&p, ctx->device));
+  const int threads = 256, blocks = p.multiProcessorCount * 4, iters = 20000;
+  double* out;
+  int rc;
+  if ((rc = ctx->get("peak", (size_t)threads * blocks, &out))) return rc;
+  fp64_peak_kernel<<<blocks, threads, 0, ctx->stream>>>(out, 100);
+  NBG_CUDA(cudaGetLastError());
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; rep++) {
+    NBG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    fp64_peak_kernel<<<blocks, threads, 0, ctx->stream>>>(out, iters);
+    NBG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    NBG_CUDA(cudaEventSynchronize(ctx->ev1));
+    float ms = 0;
+    NBG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    best = std::min(best, ms);
+  }
+  *tflops = 2.0 * (double)blocks * threads * iters * PEAK_CHAINS / (best * 1e-3) / 1e12;
+  return NBG_OK;
+}
 
 static int batch_host_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc, double* t, double* x,
                              double* v, const double* m, double* xerror, double* verror, double* jac_step,

@@ -50,6 +50,21 @@ template <class T> void store_state(const State<T>& s, double* x, double* v, dou
   if (dqdt) for (int q = 0; q < M; q++) dqdt[q] = (double)s.dqdt[q];
 }
 
+// Perturbation of the reference's tests: dq = dlnq*q (dlnq when q == 0).
+// BigFloat's 256-bit precision absorbs a relative step on a coordinate that is
+// zero up to rounding (~1e-19 next to 1e-2); binary128 does not, so the step
+// is floored at 1e-6 of the array's scale.
+static inline quad fd_step(quad q, quad dlnq, quad scale) {
+  quad a = (q < quad(0)) ? -q : q;
+  quad fl = quad(1e-6) * scale;
+  return dlnq * (a > fl ? a : (fl > quad(0) ? fl : quad(1)));
+}
+template <class T> static quad absmax(const std::vector<T>& a) {
+  quad s = quad(0);
+  for (auto q : a) { quad b = (q < T(0)) ? -quad(q) : quad(q); if (b > s) s = b; }
+  return s;
+}
+
 }  // namespace
 
 extern "C" {
@@ -214,8 +229,7 @@ int oracle_phi(int n, double h, double alpha, int which, double* x, double* v, c
 
 // ------------------------------------------------------ quad-precision pins
 
-// Perturbation rule of the reference's tests: dq = dlnq*q, or dlnq when q == 0.
-static inline quad fd_step(quad q, quad dlnq) { return (q != quad(0)) ? dlnq * q : dlnq; }
+
 
 // Numerical 14x14 Jacobian and 14 dq/dt of one no-grad kepler_driftij_gamma!
 // call (test/test_kepler_driftij_gamma.jl:60-282).  Columns follow jac_ij:
@@ -232,7 +246,8 @@ int oracle_fd_kepler_driftij(int n, int i, int j, double h, int drift_first, con
       int b = bodies[(which - 1) / 3];
       int kind = (which - 1) % 3;  // 0: x, 1: v, 2: m
       quad& q = (kind == 0) ? out.X(comp, b) : (kind == 1) ? out.V(comp, b) : out.m[b];
-      dq = fd_step(q, dlnq);
+      quad scale = (kind == 0) ? absmax(out.x) : (kind == 1) ? absmax(out.v) : absmax(out.m);
+      dq = fd_step(q, dlnq, scale);
       q = q + sign * dq;
     }
     kepler_driftij_ng(out, i, j, hh, drift_first != 0);
@@ -300,7 +315,8 @@ int oracle_fd_map_jacobian(int n, int op, double h, int64_t nsteps, const double
       load_state(sm, n, x, v, m, nullptr, nullptr, nullptr, nullptr, nullptr, pair, nullptr);
       quad* qp = (kk < 3) ? &sp.X(kk, b) : (kk < 6) ? &sp.V(kk - 3, b) : &sp.m[b];
       quad* qm = (kk < 3) ? &sm.X(kk, b) : (kk < 6) ? &sm.V(kk - 3, b) : &sm.m[b];
-      quad dq = fd_step(*qp, dlnq);
+      quad scale = (kk < 3) ? absmax(sp.x) : (kk < 6) ? absmax(sp.v) : absmax(sp.m);
+      quad dq = fd_step(*qp, dlnq, scale);
       *qp = *qp + dq;
       *qm = *qm - dq;
       apply(sp);

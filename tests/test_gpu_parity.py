@@ -1,0 +1,205 @@
+"""Parity of the CUDA path (libnbg_cuda through its C ABI) with the CPU oracle.
+
+Every case runs the same seeded inputs through nbg_integrate_transits /
+nbg_batch_integrate_transits and through the oracle's restatement of the
+reference, and compares with the tolerances of tests/parity.py.
+"""
+import numpy as np
+import pytest
+
+import nbg
+import oracle_lib as O
+import parity as P
+from conftest import has_gpu
+from nbg import workloads as W
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not has_gpu(), reason="needs a CUDA GPU")]
+
+
+def run_pair(el, h, tmax, grad=True, ti=1, t0=0.0, pair=None, H=None, masses=None):
+    """(GPU state, GPU timing, oracle state, oracle timing) for one system."""
+    ic = nbg.ElementsIC(t0, el.shape[0] if H is None else H, el)
+    s = nbg.State(ic)
+    if pair is not None:
+        s.pair[...] = pair
+    if masses is not None:
+        s.m[...] = masses
+    tt = nbg.TransitTiming(abs(tmax), ic, ti)
+    x, v, jinit = s.x.copy(order="F"), s.v.copy(order="F"), s.jac_init.copy(order="F")
+    nbg.Integrator(nbg.ahl21, h, t0, tmax)(s, tt, grad=grad)
+    so = O.OState(x, v, ic.m if masses is None else masses, jac_init=jinit, t=t0, pair=pair)
+    to = O.OTiming(ic.nbody, tt.ntt, ti - 1)
+    O.integrate_transits(so, to, h, tmax, grad=grad)
+    return s, tt, so, to
+
+
+def compare(s, tt, so, to, tmax, grad=True):
+    P.check_counts(tt.count, to.count)
+    P.check_tt(tt.tt, to.tt, to.count, tmax)
+    assert s.t[0] == so.t[0]
+    P.check_state(s, so, check_jac=grad)
+    if grad:
+        P.check_transit_derivs(tt.dtdq0, to.dtdq0, to.count, "dtdq0")
+        P.check_transit_derivs(tt.dtdelements, to.dtdelements, to.count, "dtdelements")
+
+
+def test_plain_3body_grad():
+    """The plain single-system configuration: 3 bodies, h = 0.5, 2000 steps, ~150 transits."""
+    el, h, tmax = W.plain_3body(0)
+    s, tt, so, to = run_pair(el, h, tmax)
+    assert to.count.sum() > 100
+    compare(s, tt, so, to, tmax)
+
+
+def test_grad_false_matches_grad_true_bitwise():
+    """test/test_transit_timing.jl:97 and test/test_integrator.jl:184 on the GPU path."""
+    el, h, tmax = W.plain_3body(3)
+    ic = nbg.ElementsIC(0.0, 3, el)
+    s1, s2 = nbg.State(ic), nbg.State(ic)
+    t1, t2 = nbg.TransitTiming(tmax, ic), nbg.TransitTiming(tmax, ic)
+    intr = nbg.Integrator(nbg.ahl21, h, 0.0, tmax)
+    intr(s1, t1, grad=False)
+    intr(s2, t2, grad=True)
+    assert np.array_equal(t1.tt, t2.tt) and np.array_equal(t1.count, t2.count)
+    assert np.array_equal(s1.x, s2.x) and np.array_equal(s1.v, s2.v)
+    _, _, so, to = run_pair(el, h, tmax, grad=False)
+    P.check_tt(t1.tt, to.tt, to.count, tmax)
+
+
+@pytest.mark.parametrize("n", list(range(2, 11)))
+def test_body_counts(n):
+    """Every built body count against the oracle on a short integration."""
+    els, hs, _ = W.batch_uneven(200, seed=n, nmin=n, nmax=n)
+    el, h = els[0], hs[0]
+    tmax = min(40.0, 200 * h)
+    s, tt, so, to = run_pair(el, h, tmax)
+    compare(s, tt, so, to, tmax)
+
+
+def test_eight_body_trappist_like():
+    els, h, _ = W.batch_8body(2, seed=5)
+    tmax = 60.0
+    s, tt, so, to = run_pair(els[0], h, tmax)
+    assert to.count.sum() > 20
+    compare(s, tt, so, to, tmax)
+
+
+def test_kick_pairs():
+    """pair[i,j] = true (kickfast! + phic!) for the planet pairs, Kepler for star-planet."""
+    els, hs, _ = W.batch_uneven(50, seed=11, nmin=4, nmax=4)
+    el, h = els[0], hs[0]
+    pair = np.ones((4, 4), dtype=np.uint8)
+    pair[0, :] = 0
+    pair[:, 0] = 0
+    s, tt, so, to = run_pair(el, h, 30.0, pair=pair)
+    compare(s, tt, so, to, 30.0)
+
+
+@pytest.mark.parametrize("ti", [2, 3])
+def test_other_transited_body(ti):
+    el, h, _ = W.plain_3body(4)
+    s, tt, so, to = run_pair(el, h, 300.0, ti=ti)
+    compare(s, tt, so, to, 300.0)
+
+
+def test_backward_integration():
+    """check_step (Integrator.jl:249-259): tmax < 0 integrates backward from s.t."""
+    el, h, _ = W.plain_3body(5)
+    s, tt, so, to = run_pair(el, h, -150.0)
+    compare(s, tt, so, to, 150.0)
+
+
+def test_nonzero_start_time():
+    el, h, _ = W.plain_3body(6)
+    s, tt, so, to = run_pair(el, h, 120.0, t0=7300.25)
+    compare(s, tt, so, to, 120.0)
+
+
+def test_second_call_continues_counts():
+    """A second intr(s, tt) with the same TransitTiming appends transits (count in/out)."""
+    el, h, _ = W.plain_3body(7)
+    ic = nbg.ElementsIC(0.0, 3, el)
+    s = nbg.State(ic)
+    tt = nbg.TransitTiming(400.0, ic)
+    intr = nbg.Integrator(nbg.ahl21, h, 0.0, 200.0)
+    intr(s, tt)
+    intr(s, tt)
+    x, v, jinit = ic.init_nbody()
+    so = O.OState(x, v, ic.m, jac_init=jinit)
+    to = O.OTiming(3, tt.ntt, 0)
+    O.integrate_transits(so, to, h, 200.0)
+    O.integrate_transits(so, to, h, 200.0)
+    compare(s, tt, so, to, 400.0)
+
+
+def test_ntt_overflow_counts_and_drops():
+    """Transits beyond ntt are counted but not stored (timing.jl:18-19)."""
+    el, h, tmax = W.plain_3body(8)
+    ic = nbg.ElementsIC(0.0, 3, el)
+    s = nbg.State(ic)
+    tt = nbg.TransitTiming(60.0, ic)  # sized for 60 days, integrated for 200
+    nbg.Integrator(nbg.ahl21, h, 0.0, 200.0)(s, tt)
+    x, v, jinit = ic.init_nbody()
+    so = O.OState(x, v, ic.m, jac_init=jinit)
+    to = O.OTiming(3, tt.ntt, 0)
+    O.integrate_transits(so, to, h, 200.0)
+    assert int(to.count.max()) > tt.ntt
+    compare(s, tt, so, to, 200.0)
+
+
+def test_massless_pair_reuses_previous_jacobian():
+    """Two massless bodies: kepler_driftij_gamma! returns before refilling jac_ij (ahl21.jl:713)."""
+    el, h, _ = W.plain_3body(9)
+    el4 = np.zeros((4, 7))
+    el4[:3] = el
+    el4[3] = [1e-5, 35.0, 3.0, 0.01, 0.0, np.pi / 2, 0.0]
+    masses = el4[:, 0].copy()
+    masses[2] = masses[3] = 0.0  # test particles, set on the State after the initial conditions
+    s, tt, so, to = run_pair(el4, h, 100.0, masses=masses)
+    assert np.all(np.isfinite(so.jac_step))
+    compare(s, tt, so, to, 100.0)
+
+
+def _batch_inputs(specs):
+    states, timings, hs, tms, grads = [], [], [], [], []
+    for el, h, tmax, grad in specs:
+        ic = nbg.ElementsIC(0.0, el.shape[0], el)
+        states.append(nbg.State(ic))
+        timings.append(nbg.TransitTiming(tmax, ic))
+        hs.append(h)
+        tms.append(tmax)
+        grads.append(grad)
+    return states, timings, hs, tms, grads
+
+
+def test_alone_and_in_batch_are_identical():
+    """Each system's result is bitwise the same alone and inside a mixed batch."""
+    els, hs, tms = W.batch_uneven(24, seed=21, nmin=2, nmax=6)
+    specs = [(el, h, min(tm, 60.0), bool(q % 3)) for q, (el, h, tm) in enumerate(zip(els, hs, tms))]
+    states, timings, hs, tms, grads = _batch_inputs(specs)
+    b = nbg.Batch([s.n for s in states], 0, hs, tms, [t.ntt for t in timings], grads)
+    for q in range(len(states)):
+        b.set_system(q, states[q], timings[q])
+    b.run()
+    for q in (0, 5, 11, 17, 23):
+        s1, t1, _, _, g1 = _batch_inputs([specs[q]])
+        b1 = nbg.Batch([s1[0].n], 0, hs[q], tms[q], [t1[0].ntt], grads[q])
+        b1.set_system(0, s1[0], t1[0])
+        b1.run()
+        for k in ("x", "v", "tt", "count", "jac_step", "dtdq0", "dtdelements", "dqdt"):
+            assert np.array_equal(b.view(k, q), b1.view(k, 0)), (q, k)
+
+
+def test_batch_matches_oracle():
+    els, hs, tms = W.batch_uneven(12, seed=31, nmin=2, nmax=9)
+    specs = [(el, h, min(tm, 50.0), True) for el, h, tm in zip(els, hs, tms)]
+    states, timings, hs, tms, grads = _batch_inputs(specs)
+    gs = [s.copy() for s in states]
+    status = nbg.integrate_transits_batch(gs, timings, hs, tms, True)
+    assert np.all(status == 0)
+    for q, (el, h, tmax, _) in enumerate(specs):
+        x, v, jinit = states[q].x, states[q].v, states[q].jac_init
+        so = O.OState(x, v, states[q].m, jac_init=jinit)
+        to = O.OTiming(states[q].n, timings[q].ntt, 0)
+        O.integrate_transits(so, to, h, tmax)
+        compare(gs[q], timings[q], so, to, tmax)
