@@ -259,6 +259,7 @@ def main():
     ap.add_argument("--nsys", type=int, default=None)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--chunk", type=int, default=0)
+    ap.add_argument("--spw", type=int, default=0, help="orbit producer systems per warp (0 = automatic)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--e2e-steps", type=int, default=2)
@@ -284,6 +285,8 @@ def main():
     ctx = nbg.Context(local_rank)
     if args.chunk:
         ctx.set_tuning(chunk_steps=args.chunk)
+    if args.spw:
+        ctx.set_orbit_lanes(args.spw)
     states, timings, hs, tms, nsteps = build_workload(nbg, args.workload, args.nsys, replica_seed(args.seed, rank))
     total_ss = int(sum(nsteps))
     b = make_batch(nbg, states, timings, hs, tms)
@@ -344,7 +347,7 @@ def main():
     ctx.set_profiling(True)
     step()
     ctx.set_profiling(False)
-    total_ms, orbit_ms, jac_ms = ctx.last_timing()
+    total_ms, orbit_ms, transit_ms, jac_ms = ctx.last_timing()
     n_orbit, n_jac = ctx.last_kernel_stats()
     flops = sum(flops_per_system_step(s.n) * ns for s, ns in zip(states, nsteps))
     peak = ctx.fp64_peak_tflops()
@@ -363,14 +366,15 @@ def main():
             "config": {"workload": args.workload, "nsys": len(states), "system_steps_per_pass": total_ss,
                        "grad": True, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "working set larger than L2 (operator records + jac_step)",
-                       "chunk_steps": args.chunk or 16},
+                       "chunk_steps": args.chunk or 16, "orbit_systems_per_warp": args.spw or "auto"},
             "e2e": {"value": e2e_val, "unit": "system-steps/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.mean(e2e_ms)) if e2e_ms else None},
             "gpu_launches": int(launches),
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                          "kernel": "jacobian_chunk_kernel", "peak_source": "measured live (nbg_fp64_peak, DFMA)",
-                         "launches": n_jac, "kernel_ms": jac_ms, "orbit_ms": orbit_ms, "loop_ms": total_ms},
+                         "launches": n_jac, "kernel_ms": jac_ms, "orbit_ms": orbit_ms, "transit_ms": transit_ms,
+                         "loop_ms": total_ms},
             "clocks": clocks,
         }
         if not args.no_cpu_baseline and world == 1:

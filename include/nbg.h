@@ -137,9 +137,13 @@ int nbg_set_tuning(nbg_context* ctx, int chunk_steps, int overlap);
 
 /* Device time (ms) of the last batched call's integration, measured with
  * CUDA events on the context's stream: total (chunk loop), and -- when
- * profiling is on -- the summed durations of the orbit-producer and
- * Jacobian-consumer launches.  No counterpart in the reference. */
-int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double* jacobian_ms);
+ * profiling is on -- the summed durations of the orbit-producer, transit-
+ * search and Jacobian-consumer launches.  No counterpart in the reference. */
+int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double* transit_ms, double* jacobian_ms);
+
+/* Systems per warp of the orbit producer (1..32; 0 = automatic: about two
+ * warps per SM).  A tuning knob; results do not depend on it. */
+int nbg_set_orbit_lanes(nbg_context* ctx, int systems_per_warp);
 
 /* Record an event pair around every orbit / Jacobian launch (off by default). */
 int nbg_set_profiling(nbg_context* ctx, int on);

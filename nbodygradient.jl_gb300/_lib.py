@@ -31,7 +31,7 @@ EXPORTS = (
     "nbg_create", "nbg_destroy", "nbg_last_error", "nbg_version", "nbg_device_info",
     "nbg_integrate_transits", "nbg_batch_integrate_transits", "nbg_batch_integrate_transits_device",
     "nbg_set_tuning", "nbg_last_timing", "nbg_last_launch_count", "nbg_fp64_peak",
-    "nbg_set_profiling", "nbg_last_kernel_stats",
+    "nbg_set_profiling", "nbg_last_kernel_stats", "nbg_set_orbit_lanes",
 )
 
 
@@ -89,11 +89,12 @@ def load(build_if_missing=True):
     L.nbg_batch_integrate_transits.argtypes = batch_args
     L.nbg_batch_integrate_transits_device.argtypes = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc)] + [_VP] * 16
     L.nbg_set_tuning.argtypes = [_VP, ctypes.c_int, ctypes.c_int]
-    L.nbg_last_timing.argtypes = [_VP, _D, _D, _D]
+    L.nbg_last_timing.argtypes = [_VP, _D, _D, _D, _D]
     L.nbg_last_launch_count.argtypes = [_VP]
     L.nbg_last_launch_count.restype = ctypes.c_int64
     L.nbg_fp64_peak.argtypes = [_VP, _D]
     L.nbg_set_profiling.argtypes = [_VP, ctypes.c_int]
+    L.nbg_set_orbit_lanes.argtypes = [_VP, ctypes.c_int]
     L.nbg_last_kernel_stats.argtypes = [_VP, _I64, _I64]
     _lib = L
     return L
@@ -148,12 +149,16 @@ class Context:
         check(load().nbg_set_tuning(self._h, int(chunk_steps), int(overlap)))
 
     def last_timing(self):
-        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
-        check(load().nbg_last_timing(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
-        return a.value, b.value, c.value
+        """(total, orbit, transit, jacobian) device ms of the last call."""
+        a, b, c, d = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(load().nbg_last_timing(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(d)))
+        return a.value, b.value, c.value, d.value
 
     def last_launch_count(self):
         return int(load().nbg_last_launch_count(self._h))
+
+    def set_orbit_lanes(self, systems_per_warp=0):
+        check(load().nbg_set_orbit_lanes(self._h, int(systems_per_warp)))
 
     def set_profiling(self, on=True):
         check(load().nbg_set_profiling(self._h, int(bool(on))))

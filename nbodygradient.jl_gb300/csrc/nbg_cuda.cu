@@ -179,7 +179,9 @@ struct nbg_context {
   std::map<std::string, Buf> pool;
   int chunk_steps = 16;
   int overlap = 0;
-  double last_total_ms = 0, last_orbit_ms = 0, last_jac_ms = 0;
+  int orbit_spw = 0;  // 0: automatic
+  int sm_count = 0;
+  double last_total_ms = 0, last_orbit_ms = 0, last_jac_ms = 0, last_transit_ms = 0;
   long long last_launches = 0, last_orbit_launches = 0, last_jac_launches = 0;
   int profile = 0;
   std::vector<cudaEvent_t> prof_events;  // pairs around each timed launch
@@ -226,6 +228,10 @@ const LaunchFn kOrbit[NBG_MAX_BODIES + 1] = {nullptr, nullptr, launch_orbit<2>, 
 const LaunchFn kJac[NBG_MAX_BODIES + 1] = {nullptr, nullptr, launch_jac<2>, launch_jac<3>, launch_jac<4>,
                                            launch_jac<5>, launch_jac<6>, launch_jac<7>, launch_jac<8>,
                                            launch_jac<9>, launch_jac<10>};
+const LaunchFn kTransit[NBG_MAX_BODIES + 1] = {nullptr, nullptr, launch_transit<2>, launch_transit<3>,
+                                               launch_transit<4>, launch_transit<5>, launch_transit<6>,
+                                               launch_transit<7>, launch_transit<8>, launch_transit<9>,
+                                               launch_transit<10>};
 const SeedFn kSeed[NBG_MAX_BODIES + 1] = {nullptr, nullptr, launch_seed<2>, launch_seed<3>, launch_seed<4>,
                                           launch_seed<5>, launch_seed<6>, launch_seed<7>, launch_seed<8>,
                                           launch_seed<9>, launch_seed<10>};
@@ -258,7 +264,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
               double* d_dq0, double* d_dtdel, long long* d_count, uint32_t* status_host) {
   cudaStream_t st = ctx->stream;
   ctx->last_launches = 0;
-  ctx->last_orbit_ms = ctx->last_jac_ms = 0;
+  ctx->last_orbit_ms = ctx->last_jac_ms = ctx->last_transit_ms = 0;
   // ---- offsets and groups
   std::vector<SysOff> off(nsys);
   std::vector<long long> nsteps(nsys);
@@ -323,6 +329,17 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     GroupArgs g;
     memset(&g, 0, sizeof(g));
     g.N = N; g.S = S; g.nsys = nsg; g.grad = gp.grad; g.K = K; g.kick = gp.kick;
+    // Orbit producer lanes per warp: a warp's FP64 instruction costs the same
+    // issue slot at any lane count, but the producer is latency bound, so a
+    // small batch is spread over about two warps per SM.
+    if (ctx->orbit_spw > 0) {
+      g.spw = ctx->orbit_spw;
+    } else {
+      int target = std::max(1, 2 * ctx->sm_count);
+      int want = (nsg + target - 1) / target, spw = 1;
+      while (spw < want && spw < 32) spw *= 2;
+      g.spw = spw;
+    }
     int npk = 0;
     for (int i = 0; i < N - 1; i++)
       for (int j = i + 1; j < N; j++)
@@ -335,9 +352,12 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     GET(x, 3 * N * S); GET(v, 3 * N * S); GET(xe, 3 * N * S); GET(ve, 3 * N * S); GET(m, N * S);
     GET(dqdt, 7 * N * S); GET(gsave, N * S); GET(count, N * S); GET(t0, S); GET(h, S); GET(hI, S);
     GET(nsteps, S); GET(ntt, S); GET(ti, S); GET(sysidx, S); GET(status, S);
+    g.task_cap = K * (N - 1) * S;
+    GET(task_f, (size_t)g.task_cap * (12 * N + 2)); GET(task_i, (size_t)g.task_cap * 3); GET(task_count, 1);
+    g.tgrid = std::min(((g.task_cap + 31) / 32) * 32, std::max(1, ctx->sm_count) * 4 * 32);
     if (gp.grad) {
       GET(steprec, (size_t)K * g.R * S); GET(trec, (size_t)K * (N - 1) * (7 * N + 1) * S);
-      GET(tflag, (size_t)K * (N - 1) * S); GET(scratch, (size_t)g.R * S);
+      GET(tflag, (size_t)K * (N - 1) * S); GET(tscratch, (size_t)g.R * g.tgrid);
       GET(Jint, (size_t)S * 6 * N * 7 * N); GET(Eint, (size_t)S * 6 * N * 7 * N);
     }
 #undef GET
@@ -412,8 +432,10 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     for (size_t q = 0; q < gargs.size(); q++) {
       const GroupArgs& g = gargs[q];
       if (c * K >= gmaxsteps[q]) continue;
+      NBG_CUDA(cudaMemsetAsync(g.task_count, 0, sizeof(int), st));
       if ((rc = timed(0, [&] { return kOrbit[g.N](g, (int)c, st); }))) return rc;
-      ctx->last_launches++;
+      if ((rc = timed(2, [&] { return kTransit[g.N](g, (int)c, st); }))) return rc;
+      ctx->last_launches += 2;
       ctx->last_orbit_launches++;
       if (g.grad) {
         if ((rc = timed(1, [&] { return kJac[g.N](g, (int)c, st); }))) return rc;
@@ -456,7 +478,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
   for (auto& pr : prof) {
     float e = 0;
     cudaEventElapsedTime(&e, ctx->prof_events[pr.second], ctx->prof_events[pr.second + 1]);
-    (pr.first ? ctx->last_jac_ms : ctx->last_orbit_ms) += e;
+    (pr.first == 1 ? ctx->last_jac_ms : pr.first == 2 ? ctx->last_transit_ms : ctx->last_orbit_ms) += e;
   }
   if (status_host) {
     std::fill(status_host, status_host + nsys, 0u);
@@ -529,6 +551,10 @@ int nbg_create(int device, nbg_context** out) {
   NBG_CUDA(cudaSetDevice(device));
   nbg_context* c = new nbg_context();
   c->device = device;
+  {
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, device) == cudaSuccess) c->sm_count = p.multiProcessorCount;
+  }
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
     delete c;
@@ -560,6 +586,14 @@ int nbg_set_tuning(nbg_context* ctx, int chunk_steps, int overlap) {
   return NBG_OK;
 }
 
+int nbg_set_orbit_lanes(nbg_context* ctx, int systems_per_warp) {
+  if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
+  if (systems_per_warp < 0 || systems_per_warp > 32)
+    return set_error(NBG_EINVAL, "systems_per_warp = %d not in 0..32", systems_per_warp);
+  ctx->orbit_spw = systems_per_warp;
+  return NBG_OK;
+}
+
 int nbg_set_profiling(nbg_context* ctx, int on) {
   if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
   ctx->profile = on ? 1 : 0;
@@ -573,10 +607,11 @@ int nbg_last_kernel_stats(nbg_context* ctx, int64_t* orbit_launches, int64_t* ja
   return NBG_OK;
 }
 
-int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double* jacobian_ms) {
+int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double* transit_ms, double* jacobian_ms) {
   if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
   if (total_ms) *total_ms = ctx->last_total_ms;
   if (orbit_ms) *orbit_ms = ctx->last_orbit_ms;
+  if (transit_ms) *transit_ms = ctx->last_transit_ms;
   if (jacobian_ms) *jacobian_ms = ctx->last_jac_ms;
   return NBG_OK;
 }

@@ -9,10 +9,10 @@
 // rounds on its own, as Julia evaluates them; fma() appears only where the
 // reference itself takes a fused product (Base.:^(x, 4)).
 //
-// GPU-specific structure: the six G/H series share one fused loop (each
-// series still runs its own recurrence and stops on its own exact-equality
-// test, so values are those of the separate loops) which turns six dependent
-// FP64 division chains into independent ones the scheduler can overlap.
+// GPU-specific structure: the six G/H series are evaluated as fixed-degree
+// polynomials with precomputed exact coefficients (gh_functions), which
+// removes the series' chains of dependent FP64 divisions from the per-pair
+// critical path.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -57,81 +57,82 @@ __device__ __forceinline__ double cubic1(double a, double b, double c) {
   return A + B - a3;
 }
 
+// sin and cos of |x| <= pi/4 from their Taylor series about 0 (coefficients
+// (-1)^k / (2k+1)! up to x^17 and (-1)^k / (2k)! up to x^18, Horner scheme in
+// x^2).  The truncation error at |x| = pi/4 is below 1e-19, the evaluation
+// error about one ulp; the result is checked against CUDA's sin and cos
+// (tests/test_gpu_math.py).  Outside |x| <= pi/4 CUDA's sincos is used.
+// The half-angle x = gamma / 2 of the Kepler solve is far below pi/4 for
+// bound orbits stepped at a fraction of their period.
+__device__ __forceinline__ void sincos_kepler(double x, double* s, double* c) {
+  if (fabs(x) > 0.78539816339744831) {
+    sincos(x, s, c);
+    return;
+  }
+  const double x2 = x * x;
+  double ps = 0x1.952c77030ad4ap-49;
+  ps = fma(ps, x2, -0x1.ae7f3e733b81fp-41);
+  ps = fma(ps, x2, 0x1.6124613a86d09p-33);
+  ps = fma(ps, x2, -0x1.ae64567f544e4p-26);
+  ps = fma(ps, x2, 0x1.71de3a556c734p-19);
+  ps = fma(ps, x2, -0x1.a01a01a01a01ap-13);
+  ps = fma(ps, x2, 0x1.1111111111111p-7);
+  ps = fma(ps, x2, -0x1.5555555555555p-3);
+  *s = fma(x * x2, ps, x);
+  double pc = -0x1.6827863b97d97p-53;
+  pc = fma(pc, x2, 0x1.ae7f3e733b81fp-45);
+  pc = fma(pc, x2, -0x1.93974a8c07c9dp-37);
+  pc = fma(pc, x2, 0x1.1eed8eff8d898p-29);
+  pc = fma(pc, x2, -0x1.27e4fb7789f5cp-22);
+  pc = fma(pc, x2, 0x1.a01a01a01a01ap-16);
+  pc = fma(pc, x2, -0x1.6c16c16c16c17p-10);
+  pc = fma(pc, x2, 0x1.5555555555555p-5);
+  *c = fma(x2 * x2, pc, fma(-0.5, x2, 1.0));
+}
+
 enum : int { GH_G3 = 1, GH_H1 = 2, GH_H2 = 4, GH_H3 = 8, GH_H5 = 16, GH_H6 = 32 };
 
 struct GH {
   double g3, h1, h2, h3, h5, h6;
 };
 
+// Coefficients c_n of the G3, H1, H2, H3, H5, H6 series in x2 = -sign(beta) gamma^2
+// (src/utils.jl:137-396), exact rationals rounded to double, n = 0..10.
+__device__ __constant__ double kGHCoef[6][11] = {
+    {0x1.0000000000000p+0, 0x1.999999999999ap-5, 0x1.3813813813814p-10, 0x1.1566abc011567p-16, 0x1.42cb40df7f3abp-23, 0x1.08db48ebe51c7p-30, 0x1.42df6ed66ca17p-38, 0x1.2fe15942481f8p-46, 0x1.c6ee8e9c1e203p-55, 0x1.154ab3925b815p-63, 0x1.189470e50aa13p-72},  // G3
+    {0x1.0000000000000p+0, 0x1.1111111111111p-4, 0x1.d41d41d41d41dp-10, 0x1.bbd779334ef0bp-16, 0x1.0cfeb60f94b0ep-22, 0x1.c60a33dd88c31p-30, 0x1.1a8380fb9f0d4p-37, 0x1.0e1da4acb1e32p-45, 0x1.99704d261b1cfp-54, 0x1.f82abadb8f19bp-63, 0x1.0132bcd1f4692p-71},  // H1
+    {0x1.0000000000000p+0, 0x1.999999999999ap-4, 0x1.d41d41d41d41dp-9, 0x1.1566abc011567p-14, 0x1.937e11175f095p-21, 0x1.8d48ed61d7aabp-28, 0x1.1a8380fb9f0d4p-35, 0x1.2fe15942481f8p-43, 0x1.ffcc606fa1e43p-52, 0x1.5a9d6076f261ap-60, 0x1.81cc1b3aee9dbp-69},  // H2
+    {0x1.999999999999ap-4, 0x1.8618618618618p-7, 0x1.6c16c16c16c17p-11, 0x1.acb5f228d4f9fp-16, 0x1.60cc1822382eep-21, 0x1.ae64567f544e4p-27, 0x1.952622512ec88p-33, 0x1.2f48851e5fad6p-39, 0x1.71b892ff937bap-46, 0x1.761b29cfaf6e8p-53, 0x1.3f3cc8d472c34p-60},  // H3
+    {0x1.1111111111111p-6, 0x1.a01a01a01a01ap-11, 0x1.1566abc011567p-16, 0x1.ae64567f544e4p-23, 0x1.b96d79892884cp-30, 0x1.42df6ed66ca17p-37, 0x1.6286e822a97a1p-45, 0x1.2f49b46814157p-53, 0x1.9ff00d5b89420p-62, 0x1.d3a2117dbc620p-71, 0x1.b6f39affec388p-80},  // H5
+    {0x1.999999999999ap-6, 0x1.5f15f15f15f16p-9, 0x1.18de5ab277f45p-13, 0x1.1a71d8c38f535p-18, 0x1.91b806e381809p-24, 0x1.adeb42b5c3e58p-30, 0x1.68045a5f7c07ap-36, 0x1.e535756d08617p-43, 0x1.0ce18de28b3bep-49, 0x1.f2cdf899367f3p-57, 0x1.88e826fd0f0dep-64},  // H6
+};
+
+__device__ __forceinline__ double gh_horner(const double* c, double x2) {
+  double p = c[10];
+#pragma unroll
+  for (int n = 9; n >= 0; n--) p = fma(p, x2, c[n]);
+  return p;
+}
+
 // G3, H1, H2, H3, H5, H6 at (gamma, beta) -- the subset named by NEED.
-// gamma < 0.5: series (utils.jl:137-165, 180-209, 225-254, 271-303, 320-349,
-// 364-396) advanced in one loop; otherwise the closed forms of utils.jl.
+// gamma < 0.5: the series of utils.jl:137-396 in x2 = -sign(beta) gamma^2,
+// |x2| < 0.25, evaluated as degree-10 polynomials with the exact series
+// coefficients (terms beyond n = 10 are below 1e-17 of the leading term).
+// The reference sums term by term until the partial sum stops changing;
+// the polynomial reaches the same value to rounding, without the series'
+// dependent FP64 divisions.  gamma >= 0.5: the closed forms of utils.jl.
 template <int NEED>
 __device__ __forceinline__ GH gh_functions(double gamma, double beta, double sqb) {
   GH o;
   o.g3 = o.h1 = o.h2 = o.h3 = o.h5 = o.h6 = 0.0;
   if (gamma < 0.5) {
-    double x2 = (-jsign(beta)) * (gamma * gamma);
-    double tg = 1.0, g3 = 1.0, g31 = 2.0, g32 = 2.0;
-    double t1 = 1.0, h1 = 1.0, h11 = 2.0, h12 = 2.0;
-    double t2 = 1.0, h2 = 1.0, h21 = 2.0, h22 = 2.0;
-    double t3 = 1.0 / 30.0, h3 = 1.0 / 10.0, h31 = 2.0 * h3, h32 = 2.0 * h3, f3 = 4.0;
-    double t5 = 1.0 / 60.0, h5 = t5, h51 = 2.0 * h5, h52 = 2.0 * h5;
-    double t6 = 1.0 / 360.0, h6 = 1.0 / 40.0, h61 = 2.0 * h6, h62 = 2.0 * h6, f6 = 16.0;
-    bool dg = !(NEED & GH_G3), d1 = !(NEED & GH_H1), d2 = !(NEED & GH_H2);
-    bool d3 = !(NEED & GH_H3), d5 = !(NEED & GH_H5), d6 = !(NEED & GH_H6);
-    for (int n = 1; n <= 100; n++) {
-      if (!dg) {
-        g32 = g31; g31 = g3;
-        tg = tg * (x2 / (double)((2 * n + 3) * (2 * n + 2)));
-        g3 = g3 + tg;
-        dg = (n >= 100) || g3 == g32 || g3 == g31;
-      }
-      if (!d1) {
-        h12 = h11; h11 = h1;
-        t1 = t1 * (x2 * (double)(n + 1));
-        t1 = t1 / (double)((2 * n + 4) * (2 * n + 3) * n);
-        h1 = h1 + t1;
-        d1 = (n >= 100) || h1 == h12 || h1 == h11;
-      }
-      if (!d2) {
-        h22 = h21; h21 = h2;
-        t2 = t2 * x2;
-        t2 = t2 / (double)((4 * n + 6) * n);
-        h2 = h2 + t2;
-        d2 = (n >= 100) || h2 == h22 || h2 == h21;
-      }
-      if (!d3) {
-        h32 = h31; h31 = h3;
-        t3 = t3 * x2;
-        t3 = t3 / (double)((2 * n + 4) * (2 * n + 5));
-        f3 = f3 * 4.0;
-        h3 = h3 + t3 * (f3 - 1.0);
-        d3 = (n >= 100) || h3 == h32 || h3 == h31;
-      }
-      if (!d5) {
-        h52 = h51; h51 = h5;
-        t5 = t5 * (x2 * (double)(n + 1));
-        t5 = t5 / (double)((2 * n + 5) * (2 * n + 4) * n);
-        h5 = h5 + t5;
-        d5 = (n >= 100) || h5 == h52 || h5 == h51;
-      }
-      if (!d6) {
-        h62 = h61; h61 = h6;
-        t6 = t6 * x2;
-        t6 = t6 / (double)((2 * n + 5) * (2 * n + 6));
-        f6 = f6 * 4.0;
-        h6 = h6 + t6 * (f6 - (double)(3 * n) - 7.0);
-        d6 = (n >= 100) || h6 == h62 || h6 == h61;
-      }
-      if (dg && d1 && d2 && d3 && d5 && d6) break;
-    }
-    if (NEED & GH_G3) o.g3 = g3 * (((-x2) * gamma) / ((6.0 * beta) * sqb));
-    if (NEED & GH_H1) o.h1 = h1 * ((x2 * x2) / (12.0 * (beta * beta)));
-    if (NEED & GH_H2) o.h2 = h2 * (((-x2) * gamma) / ((3.0 * beta) * sqb));
-    if (NEED & GH_H3) o.h3 = h3 * (((-(x2 * x2)) * gamma) / (beta * sqb));
-    if (NEED & GH_H5) o.h5 = h5 * (((-(x2 * x2)) * gamma) / (beta * sqb));
-    if (NEED & GH_H6) o.h6 = h6 * ((-(x2 * x2 * x2)) / (beta * beta));
+    const double x2 = (-jsign(beta)) * (gamma * gamma);
+    if (NEED & GH_G3) o.g3 = gh_horner(kGHCoef[0], x2) * (((-x2) * gamma) / ((6.0 * beta) * sqb));
+    if (NEED & GH_H1) o.h1 = gh_horner(kGHCoef[1], x2) * ((x2 * x2) / (12.0 * (beta * beta)));
+    if (NEED & GH_H2) o.h2 = gh_horner(kGHCoef[2], x2) * (((-x2) * gamma) / ((3.0 * beta) * sqb));
+    if (NEED & GH_H3) o.h3 = gh_horner(kGHCoef[3], x2) * (((-(x2 * x2)) * gamma) / (beta * sqb));
+    if (NEED & GH_H5) o.h5 = gh_horner(kGHCoef[4], x2) * (((-(x2 * x2)) * gamma) / (beta * sqb));
+    if (NEED & GH_H6) o.h6 = gh_horner(kGHCoef[5], x2) * ((-(x2 * x2 * x2)) / (beta * beta));
   } else if (beta >= 0.0) {
     double s, c;
     sincos(gamma, &s, &c);
@@ -204,7 +205,7 @@ __device__ __noinline__ void kep_delxv(const double* x0, const double* v0, doubl
     gamma1 = gamma;
     double xx = 0.5 * gamma;
     if (beta0 > 0.0) {
-      sincos(xx, &sx, &cx);
+      sincos_kepler(xx, &sx, &cx);
     } else {
       sx = sinh(xx);
       cx = exp(-xx) + sx;
@@ -217,7 +218,7 @@ __device__ __noinline__ void kep_delxv(const double* x0, const double* v0, doubl
   P.newton_iter = iter;
   double xx = 0.5 * gamma;
   if (beta0 > 0.0) {
-    sincos(xx, &sx, &cx);
+    sincos_kepler(xx, &sx, &cx);
   } else {
     sx = sinh(xx);
     cx = exp(-xx) + sx;
@@ -263,6 +264,8 @@ __device__ __noinline__ void kep_jacobian(const KepParams& P, const double* x0, 
   const double dfdt = P.dfdt, fm1 = P.fm1, gmh = P.gmh, dgdtm1 = P.dgdtm1, r0 = P.r0, r = P.r;
   const double r0inv = P.r0inv, rinv = P.rinv, k = P.k, h = P.h, beta = P.beta, betainv = P.betainv;
   const double eta = P.eta, sqb = P.sqb, zeta = P.zeta;
+  // repeated divisors of the reference's expressions, inverted once
+  const double g1inv = 1.0 / g1, g2inv = 1.0 / g2, kinv = 1.0 / k;
   double r0inv2 = r0inv * r0inv;
   double r0inv3 = r0inv2 * r0inv;
   double rinv2 = rinv * rinv;
@@ -283,13 +286,13 @@ __device__ __noinline__ void kep_jacobian(const KepParams& P, const double* x0, 
     double c13 = g1 * h - g2 * r0;
     double c9 = 2.0 * g2 * h - 3.0 * g3 * r0;
     double c10 = k * (r0inv2 * r0inv2) * ((-g2) * r0 * h + k * c9 * betainv - c3 * c13 * rinv);
-    double c24 = r0inv3 * (r0 * (2.0 * k * r0inv - beta) * betainv - g1 * c3 * rinv / g2);
+    double c24 = r0inv3 * (r0 * (2.0 * k * r0inv - beta) * betainv - g1 * c3 * rinv * g2inv);
     dfm1dxx = fm1 * c24;
     dfm1dxv = (-fm1) * (g1 * rinv + h * c24);
     dfm1dvx = dfm1dxv;
-    dfm1dvv = fm1 * rinv * ((-r0) * g2 + k * h6 * betainv / g2 + h * (2.0 * g1 + h * r * c24));
-    dfm1dh = fm1 * (g1 * rinv * (1.0 / g2 + 2.0 * k * r0inv - beta) - eta * c24);
-    dfm1dk = fm1 * (1.0 / k + g1 * c1 * rinv * r0inv / g2 - 2.0 * betainv * r0inv);
+    dfm1dvv = fm1 * rinv * ((-r0) * g2 + k * h6 * betainv * g2inv + h * (2.0 * g1 + h * r * c24));
+    dfm1dh = fm1 * (g1 * rinv * (g2inv + 2.0 * k * r0inv - beta) - eta * c24);
+    dfm1dk = fm1 * (kinv + g1 * c1 * rinv * r0inv * g2inv - 2.0 * betainv * r0inv);
     double h4 = (-P.H1v) * beta;
     dfm1dk2 = (r0 * h4 + k * h6);
     dgmhdxx = c10;
@@ -304,9 +307,9 @@ __device__ __noinline__ void kep_jacobian(const KepParams& P, const double* x0, 
                (g1 * h6 + g3 * h4) * k * r0);
     double c12 = g0 * h - g1 * r0;
     double c17 = r0 - r - g2 * k;
-    double c21 = (g2 * k - r0) * (beta * c3 - k * g1 * r) * betainv * rinv2 * r0inv3 / g1 +
+    double c21 = (g2 * k - r0) * (beta * c3 - k * g1 * r) * betainv * rinv2 * r0inv3 * g1inv +
                  eta * g1 * rinv * r0inv2 - 2.0 * r0inv2;
-    double c22 = rinv * ((-g1) - g0 * g2 / g1 + g2 * c2 * rinv);
+    double c22 = rinv * ((-g1) - g0 * g2 * g1inv + g2 * c2 * rinv);
     double c25 = k * rinv * r0inv2 *
                  ((-g2) + k * (c13 - g2 * r0) * betainv * r0inv2 - c13 * r0inv - c12 * c3 * rinv * r0inv2 +
                   c13 * c2 * c3 * rinv2 * r0inv2 - c13 * (k * (g2 * k + r) - g0 * r0 * zeta) * betainv * rinv * r0inv2);
@@ -317,13 +320,13 @@ __device__ __noinline__ void kep_jacobian(const KepParams& P, const double* x0, 
     double c34 = ((-beta) * (eta * eta) * (g2 * g2) - eta * k * h8 - h6 * ksq - 2.0 * beta * eta * r0 * g1 * g2 +
                   ((g2 * g2) - 3.0 * g1 * g3) * beta * k * r0 - beta * (g1 * g1) * (r0 * r0)) *
                      betainv * rinv2 +
-                 (eta * (g2 * g2)) * rinv / g1 + (k * h8) * betainv * rinv / g1;
+                 (eta * (g2 * g2)) * rinv * g1inv + (k * h8) * betainv * rinv * g1inv;
     ddfdtdvv = dfdt * (c34 - 2.0 * h * c22 + hsq * c21);
-    ddfdtdk = dfdt * (1.0 / k - betainv * r0inv - c17 * betainv * rinv * r0inv -
-                      c1 * (g1 * c2 - g0 * r) * rinv2 * r0inv / g1);
+    ddfdtdk = dfdt * (kinv - betainv * r0inv - c17 * betainv * rinv * r0inv -
+                      c1 * (g1 * c2 - g0 * r) * rinv2 * r0inv * g1inv);
     ddfdtdk2 = (-(g2 * k - r0)) * (beta * r0 * (g3 - g1 * g2) - beta * eta * (g2 * g2) + k * h3) * betainv * rinv2 *
                r0inv;
-    ddfdtdh = dfdt * (g0 * rinv / g1 - c2 * rinv2 - (2.0 * k * r0inv - beta) * c22 - eta * c21);
+    ddfdtdh = dfdt * (g0 * rinv * g1inv - c2 * rinv2 - (2.0 * k * r0inv - beta) * c22 - eta * c21);
     dgdxx = c25;
     dgdxv = c26 - h * c25;
     dgdvx = c26 - h * c25;
@@ -348,7 +351,7 @@ __device__ __noinline__ void kep_jacobian(const KepParams& P, const double* x0, 
     const double h2 = P.h2;
     double c14 = r0 * g2 - k * h1;
     double c15 = eta * h1 + h2 * r0;
-    double c16 = eta * h2 + g1 * gamma * r0 / sqb;
+    double c16 = eta * h2 + g1 * gamma * r0 * (1.0 / sqb);
     double c17 = r0 - r - g2 * k;
     double c19 = 4.0 * eta * h1 + 3.0 * h2 * r0;
     double c23 = h2 * k - r0 * g1;
@@ -401,18 +404,18 @@ __device__ __noinline__ void kep_jacobian(const KepParams& P, const double* x0, 
                       beta * (beta * g1 * g3 - g2) * (r0 * r0)));
     dgmhdh = k * rinv3 * (r * c16 - c2 * c15);
     ddfdtdxx = dfdt *
-               (eta * g1 * rinv - 2.0 - g0 * c3 * rinv * r0inv / g1 + c2 * c3 * r0inv * rinv2 -
+               (eta * g1 * rinv - 2.0 - g0 * c3 * rinv * r0inv * g1inv + c2 * c3 * r0inv * rinv2 -
                 k * (k * g2 - r0) * betainv * rinv * r0inv) *
                r0inv2;
-    ddfdtdxv = (-dfdt) * (g0 * g2 / g1 + (r0 * g1 + eta * g2) * rinv) * rinv;
+    ddfdtdxv = (-dfdt) * (g0 * g2 * g1inv + (r0 * g1 + eta * g2) * rinv) * rinv;
     ddfdtdvx = ddfdtdxv;
     ddfdtdvv = (-k) * rinv3 * r0inv * betainv *
                ((beta * eta * (g2 * g2) + k * h8) * (r0 * g0 + k * g2) +
                 g1 * ((-h6) * ksq + ((-(2.0 * eta)) * g1 * g2 + (h1 - 2.0 * g1 * g3) * k) * beta * r0 -
                       beta * (g1 * g1) * (r0 * r0)));
-    ddfdtdk = dfdt * (1.0 / k + c1 * (r0 - g2 * k) * r0inv * rinv2 / g1 - betainv * r0inv * (1.0 + c17 * rinv));
+    ddfdtdk = dfdt * (kinv + c1 * (r0 - g2 * k) * r0inv * rinv2 * g1inv - betainv * r0inv * (1.0 + c17 * rinv));
     ddfdtdk2 = (r0 - g2 * k) * betainv * r0inv * rinv2 * ((-eta) * beta * (g2 * g2) + h3 * k + (g3 - g1 * g2) * beta * r0);
-    ddfdtdh = dfdt * (r0 - g2 * k) * rinv2 / g1;
+    ddfdtdh = dfdt * (r0 - g2 * k) * rinv2 * g1inv;
     dgdxx = rinv2 * r0inv3 *
             ((eta * g2 + g1 * r0) * k * c3 * rinv + g2 * k * (k * (g2 * k - r) - g0 * r0 * zeta) * betainv);
     dgdxv = k * g2 * rinv3 * (r * g1 + r0 * g1 + eta * g2);

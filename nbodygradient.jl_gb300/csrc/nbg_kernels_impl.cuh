@@ -20,7 +20,8 @@ namespace nbg {
 // Orbit producer for one chunk of K steps of one group (one lane per system).
 template <int N>
 __global__ void __launch_bounds__(PROD_BS) orbit_chunk_kernel(GroupArgs g, int chunk) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((int)threadIdx.x >= g.spw) return;
+  const int s = blockIdx.x * g.spw + threadIdx.x;
   if (s >= g.S || g.sysidx[s] < 0) return;
   const int S = g.S;
   const long long nst = g.nsteps[s];
@@ -45,7 +46,6 @@ __global__ void __launch_bounds__(PROD_BS) orbit_chunk_kernel(GroupArgs g, int c
   const double t0 = g.t0[s], h = g.h[s], hI = g.hI[s];
   const int ntt = g.ntt[s], ti = g.ti[s];
   const uint64_t kick = g.kick;
-  const int gsys = g.sysidx[s];
   unsigned int status = g.status[s];
   for (int kk = 0; kk < g.K; kk++) {
     const long long istep = k0 + kk;
@@ -58,68 +58,38 @@ __global__ void __launch_bounds__(PROD_BS) orbit_chunk_kernel(GroupArgs g, int c
       ahl21_step<N, false, false>(st, w, h, kick, Rec{nullptr, 0});
     }
     const double t = t0 + (double)(istep + 1) * h;
-    // detect_transits! (timing.jl:3-28); the state after detection is the
-    // state before it (set_state!(s, s_prior)), so the search works on copies.
+    // detect_transits! (timing.jl:3-28).  The search itself (findtransit!) is
+    // queued: it runs from a copy of this state in transit_kernel, with full
+    // warps, instead of stalling the 31 other systems of this warp.
     for (int o = 0; o < N - 1; o++) {
       const int ib = (o < ti) ? o : o + 1;
       const double gi = gsky(st, ib, ti);
       const double xi = st.x[3 * ib], yi = st.x[3 * ib + 1], zi = st.x[3 * ib + 2];
       const double ri = sqrt(xi * xi + yi * yi + zi * zi);
-      int flag = -1;
+      if (g.grad) g.tflag[(size_t)(kk * (N - 1) + o) * S + s] = -1;
       if (gi > 0.0 && gsave[ib] < 0.0 && -zi > 0.25 * ri && ri < 1e12) {
         count[ib] += 1;
         if (count[ib] <= ntt) {
-          // findtransit! (timing.jl:31-109)
-          double dt0 = -gi * hI / (gi - gsave[ib]);
-          double stmp = 0.0, tt1 = dt0 + 1.0, tt2 = dt0 + 2.0;
-          int iter = 0;
-          Sys<N> wk;
-          while (true) {
-            tt2 = tt1;
-            tt1 = dt0;
-            wk = st;
-            ahl21_step<N, true, true>(wk, w, dt0, kick, Rec{nullptr, 0});
-            const double gs = gsky(wk, ti, ib);
-            const double gd = gdot(wk, ti, ib);
-            const double dt = -gs / gd;
-            kahan(dt0, stmp, dt);
-            iter += 1;
-            if (iter >= 20 || dt0 == tt1 || dt0 == tt2) break;
+          const int idx = atomicAdd(g.task_count, 1);
+          if (idx < g.task_cap) {  // the capacity is the number of (step, occultor, system) slots
+            double* tf = g.task_f + (size_t)idx * (12 * N + 2);
+            for (int q = 0; q < 3 * N; q++) {
+              tf[q] = st.x[q];
+              tf[3 * N + q] = st.v[q];
+              tf[6 * N + q] = st.xe[q];
+              tf[9 * N + q] = st.ve[q];
+            }
+            tf[12 * N] = -gi * hI / (gi - gsave[ib]);  // first estimate (timing.jl:20)
+            tf[12 * N + 1] = t;
+            int* tk = g.task_i + 3 * idx;
+            tk[0] = s;
+            tk[1] = kk * (N - 1) + o;
+            tk[2] = (int)(count[ib] - 1);
           }
-          if (iter >= 20) status |= NBG_STATUS_NEWTON_ITMAX;
-          const long long c = count[ib] - 1;
-          if (g.grad) {
-            wk = st;
-            Rec rec{g.scratch + s, S};
-            ahl21_step<N, true, true>(wk, w, dt0, kick, rec);
-            // dtbvdq! row 1 (timing.jl:155-171) as u^T jac_step with
-            // u^T = w^T S(dt0): w holds dg/dq at the transit, S the partial
-            // step's map on jac_step.  The consumer forms u^T J per column.
-            double u[7 * N];
-            for (int q = 0; q < 7 * N; q++) u[q] = 0.0;
-            const double dvx = wk.v[3 * ib] - wk.v[3 * ti], dvy = wk.v[3 * ib + 1] - wk.v[3 * ti + 1];
-            const double dx = wk.x[3 * ib] - wk.x[3 * ti], dy = wk.x[3 * ib + 1] - wk.x[3 * ti + 1];
-            u[7 * ib + 0] = dvx;
-            u[7 * ti + 0] = -dvx;
-            u[7 * ib + 1] = dvy;
-            u[7 * ti + 1] = -dvy;
-            u[7 * ib + 3] = dx;
-            u[7 * ti + 3] = -dx;
-            u[7 * ib + 4] = dy;
-            u[7 * ti + 4] = -dy;
-            adjoint_step<N>(u, dt0, kick, rec);
-            const double gd = gdot(wk, ti, ib);
-            double* tr = g.trec + ((size_t)(kk * (N - 1) + o) * (7 * N + 1)) * S + s;
-            for (int q = 0; q < 7 * N; q++) tr[(size_t)q * S] = u[q];
-            tr[(size_t)(7 * N) * S] = gd;
-            flag = (int)c;
-          }
-          g.tt[g.off_tt[gsys] + ib + (long long)N * c] = t + dt0;
         } else {
           status |= NBG_STATUS_NTT_OVERFLOW;
         }
       }
-      if (g.grad) g.tflag[(size_t)(kk * (N - 1) + o) * S + s] = flag;
       gsave[ib] = gi;
     }
   }
@@ -136,6 +106,82 @@ __global__ void __launch_bounds__(PROD_BS) orbit_chunk_kernel(GroupArgs g, int c
     g.count[q * S + s] = count[q];
   }
   g.status[s] = status;
+}
+
+
+// findtransit! (src/transits/timing.jl:31-109) for the searches the orbit
+// producer queued in this chunk: Newton iterations on partial AHL21 steps
+// from the end-of-step state, then (grad) the partial step at the converged
+// dt0 with its operator records and the adjoint row u^T = w^T S(dt0) that the
+// Jacobian consumer turns into dtdq0 (dtbvdq! row 1, timing.jl:155-171).
+// One lane per search, grid-stride over the queue.
+template <int N>
+__global__ void __launch_bounds__(TRANSIT_BS) transit_kernel(GroupArgs g, int chunk) {
+  const int ntask = min(*g.task_count, g.task_cap);
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int G = gridDim.x * blockDim.x;
+  const int S = g.S;
+  Work<N> w;
+  for (int idx = tid; idx < ntask; idx += G) {
+    const int* tk = g.task_i + 3 * idx;
+    const int s = tk[0], slot = tk[1], c = tk[2];
+    const int o = slot % (N - 1);
+    const int ti = g.ti[s];
+    const int ib = (o < ti) ? o : o + 1;
+    const double* tf = g.task_f + (size_t)idx * (12 * N + 2);
+    Sys<N> st;
+    for (int q = 0; q < 3 * N; q++) {
+      st.x[q] = tf[q];
+      st.v[q] = tf[3 * N + q];
+      st.xe[q] = tf[6 * N + q];
+      st.ve[q] = tf[9 * N + q];
+    }
+    for (int q = 0; q < N; q++) st.m[q] = g.m[q * S + s];
+    for (int q = 0; q < 7 * N; q++) st.dqdt[q] = 0.0;
+    double dt0 = tf[12 * N];
+    const double t = tf[12 * N + 1];
+    const uint64_t kick = g.kick;
+    double stmp = 0.0, tt1 = dt0 + 1.0, tt2 = dt0 + 2.0;
+    int iter = 0;
+    Sys<N> wk;
+    while (true) {
+      tt2 = tt1;
+      tt1 = dt0;
+      wk = st;
+      ahl21_step<N, true, true>(wk, w, dt0, kick, Rec{nullptr, 0});
+      const double gs = gsky(wk, ti, ib);
+      const double gd = gdot(wk, ti, ib);
+      const double dt = -gs / gd;
+      kahan(dt0, stmp, dt);
+      iter += 1;
+      if (iter >= 20 || dt0 == tt1 || dt0 == tt2) break;
+    }
+    if (iter >= 20) atomicOr(g.status + s, NBG_STATUS_NEWTON_ITMAX);
+    if (g.grad) {
+      wk = st;
+      Rec rec{g.tscratch + tid, G};
+      ahl21_step<N, true, true>(wk, w, dt0, kick, rec);
+      double u[7 * N];
+      for (int q = 0; q < 7 * N; q++) u[q] = 0.0;
+      const double dvx = wk.v[3 * ib] - wk.v[3 * ti], dvy = wk.v[3 * ib + 1] - wk.v[3 * ti + 1];
+      const double dx = wk.x[3 * ib] - wk.x[3 * ti], dy = wk.x[3 * ib + 1] - wk.x[3 * ti + 1];
+      u[7 * ib + 0] = dvx;
+      u[7 * ti + 0] = -dvx;
+      u[7 * ib + 1] = dvy;
+      u[7 * ti + 1] = -dvy;
+      u[7 * ib + 3] = dx;
+      u[7 * ti + 3] = -dx;
+      u[7 * ib + 4] = dy;
+      u[7 * ti + 4] = -dy;
+      adjoint_step<N>(u, dt0, kick, rec);
+      const double gd = gdot(wk, ti, ib);
+      double* tr = g.trec + ((size_t)slot * (7 * N + 1)) * S + s;
+      for (int q = 0; q < 7 * N; q++) tr[(size_t)q * S] = u[q];
+      tr[(size_t)(7 * N) * S] = gd;
+      g.tflag[(size_t)slot * S + s] = c;
+    }
+    g.tt[g.off_tt[g.sysidx[s]] + ib + (long long)N * c] = t + dt0;
+  }
 }
 
 // Jacobian consumer for one chunk of K steps (one lane per column).
@@ -211,7 +257,7 @@ __global__ void seed_gsave_kernel(GroupArgs g) {
 
 template <int N>
 int launch_orbit(const GroupArgs& g, int chunk, cudaStream_t st) {
-  int blocks = (g.S + PROD_BS - 1) / PROD_BS;
+  int blocks = (g.S + g.spw - 1) / g.spw;
   orbit_chunk_kernel<N><<<blocks, PROD_BS, 0, st>>>(g, chunk);
   return 0;
 }
@@ -227,6 +273,12 @@ int launch_jac(const GroupArgs& g, int chunk, cudaStream_t st) {
     attr_set = true;
   }
   jacobian_chunk_kernel<N><<<blocks, CONS_BS, smem, st>>>(g, chunk);
+  return 0;
+}
+
+template <int N>
+int launch_transit(const GroupArgs& g, int chunk, cudaStream_t st) {
+  transit_kernel<N><<<g.tgrid / TRANSIT_BS, TRANSIT_BS, 0, st>>>(g, chunk);
   return 0;
 }
 

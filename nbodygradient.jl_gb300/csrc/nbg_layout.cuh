@@ -21,11 +21,13 @@ __host__ __device__ inline int step_record_size(int N, int npk, bool kick) {
   return (kick ? 2 * op_size(N) : 0) + 2 * npk * PREC + op_size(N);
 }
 
-constexpr int PROD_BS = 32;   // orbit producer: one warp per block, spread over SMs
-constexpr int CONS_BS = 128;  // Jacobian consumer: four warps per block
+constexpr int PROD_BS = 32;     // orbit producer: one warp per block, spread over SMs
+constexpr int CONS_BS = 128;    // Jacobian consumer: four warps per block
+constexpr int TRANSIT_BS = 32;  // transit searches: one warp per block
 
 struct GroupArgs {
   int N, S, nsys, grad, K, R, npk;
+  int spw;  // orbit producer: systems per warp (lanes >= spw idle)
   unsigned long long kick;
   // per-system state, structure of arrays: element e of system s at [e * S + s]
   double *x, *v, *xe, *ve, *m, *dqdt, *gsave;
@@ -43,13 +45,20 @@ struct GroupArgs {
   double* steprec;  // [K][R][S]
   double* trec;     // [K][N-1][7N+1][S]
   int* tflag;       // [K][N-1][S]
-  double* scratch;  // [R][S]
   // consumer state: non-mass rows of jac_step / jac_error, [S][6N][7N]
   double *Jint, *Eint;
+  // transit searches queued by the orbit producer for the transit kernel
+  double* task_f;   // [task_cap][12N + 2]: x, v, xerror, verror, first dt0, t
+  int* task_i;      // [task_cap][3]: system, slot kk*(N-1)+o, transit index
+  int* task_count;  // tasks queued in this chunk
+  int task_cap;
+  double* tscratch;  // [R][tgrid]: operator records of a search's final partial step
+  int tgrid;         // threads of the transit kernel
 };
 
 template <int N> int launch_orbit(const GroupArgs& g, int chunk, cudaStream_t st);
 template <int N> int launch_jac(const GroupArgs& g, int chunk, cudaStream_t st);
 template <int N> int launch_seed(const GroupArgs& g, cudaStream_t st);
+template <int N> int launch_transit(const GroupArgs& g, int chunk, cudaStream_t st);
 
 }  // namespace nbg

@@ -71,6 +71,9 @@ extern "C" {
 
 int oracle_version(void) { return 1; }
 
+// Transit Newton searches that stopped at ITMAX on this thread so far.
+long long oracle_newton_itmax_hits(void) { return newton_itmax_hits(); }
+
 // ElementsIC(t0, H, elements) -> init_nbody.  H may be NULL (fully nested).
 int oracle_init_nbody(int n, double t0, const double* elements, const double* H, double* x, double* v,
                       double* jac_init) {

@@ -58,6 +58,13 @@ template <class T> void dtbvdq1(State<T>& s, int i, int j, std::vector<T>& dtdq)
   }
 }
 
+// Number of transit Newton searches that stopped at ITMAX (diagnostics only;
+// the reference continues silently).
+inline long long& newton_itmax_hits() {
+  static thread_local long long n = 0;
+  return n;
+}
+
 // findtransit! (timing.jl:31-109), TransitTiming branch
 template <class T>
 void findtransit(int i, int j, T dt0, State<T>& s, Derivs<T>& d, TransitTiming<T>& tt, bool grad) {
@@ -80,6 +87,7 @@ void findtransit(int i, int j, T dt0, State<T>& s, Derivs<T>& d, TransitTiming<T
     iter += 1;
     if (iter >= ITMAX || dt0 == tt1 || dt0 == tt2) break;
   }
+  if (iter >= ITMAX) newton_itmax_hits() += 1;
   if (grad) {
     set_state(s, tt.s_prior);
     d.zero();

@@ -55,7 +55,7 @@ def test_version_and_error_buffer():
 def test_null_arguments_are_rejected_without_a_gpu():
     L = nbg._lib.load()
     assert L.nbg_set_tuning(None, 16, 0) == nbg._lib.NBG_EINVAL
-    assert L.nbg_last_timing(None, None, None, None) == nbg._lib.NBG_EINVAL
+    assert L.nbg_last_timing(None, None, None, None, None) == nbg._lib.NBG_EINVAL
     assert L.nbg_integrate_transits(None, 3, 0, 0.5, 10.0, 1, *([None] * 11), 10, None, None, None, None) \
         == nbg._lib.NBG_EINVAL
     assert "NULL" in nbg._lib.last_error()

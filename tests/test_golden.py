@@ -27,7 +27,7 @@ def _check(g, tt, dtdq0, dtdel, count, x, v, jac, dqdt, t):
     P.check_counts(count, g["count"])
     P.check_tt(tt, g["tt"], g["count"], float(g["tmax"]))
     P.check_transit_derivs(dtdq0, g["dtdq0"], g["count"])
-    P.check_transit_derivs(dtdel, g["dtdelements"], g["count"], "dtdelements")
+    P.check_transit_derivs(dtdel, g["dtdelements"], g["count"], "dtdelements", g["dtdq0"], g["jac_init"])
     gs, rs = _S(), _S()
     gs.x, gs.v, gs.jac_step, gs.dqdt = x, v, jac, dqdt
     rs.x, rs.v, rs.jac_step, rs.dqdt = g["x"], g["v"], g["jac_step"], g["dqdt"]

