@@ -181,7 +181,7 @@ struct nbg_context {
   int overlap = 0;
   int orbit_spw = 0;  // 0: automatic
   int sm_count = 0;
-  double last_total_ms = 0, last_orbit_ms = 0, last_jac_ms = 0, last_transit_ms = 0;
+  double last_total_ms = 0, last_orbit_ms = 0, last_jac_ms = 0, last_transit_ms = 0, last_ops_ms = 0;
   long long last_launches = 0, last_orbit_launches = 0, last_jac_launches = 0;
   int profile = 0;
   std::vector<cudaEvent_t> prof_events;  // pairs around each timed launch
@@ -232,6 +232,10 @@ const LaunchFn kTransit[NBG_MAX_BODIES + 1] = {nullptr, nullptr, launch_transit<
                                                launch_transit<4>, launch_transit<5>, launch_transit<6>,
                                                launch_transit<7>, launch_transit<8>, launch_transit<9>,
                                                launch_transit<10>};
+const LaunchFn kOps[NBG_MAX_BODIES + 1] = {nullptr, nullptr, launch_operators<2>, launch_operators<3>,
+                                           launch_operators<4>, launch_operators<5>, launch_operators<6>,
+                                           launch_operators<7>, launch_operators<8>, launch_operators<9>,
+                                           launch_operators<10>};
 const SeedFn kSeed[NBG_MAX_BODIES + 1] = {nullptr, nullptr, launch_seed<2>, launch_seed<3>, launch_seed<4>,
                                           launch_seed<5>, launch_seed<6>, launch_seed<7>, launch_seed<8>,
                                           launch_seed<9>, launch_seed<10>};
@@ -264,7 +268,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
               double* d_dq0, double* d_dtdel, long long* d_count, uint32_t* status_host) {
   cudaStream_t st = ctx->stream;
   ctx->last_launches = 0;
-  ctx->last_orbit_ms = ctx->last_jac_ms = ctx->last_transit_ms = 0;
+  ctx->last_orbit_ms = ctx->last_jac_ms = ctx->last_transit_ms = ctx->last_ops_ms = 0;
   // ---- offsets and groups
   std::vector<SysOff> off(nsys);
   std::vector<long long> nsteps(nsys);
@@ -358,6 +362,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     if (gp.grad) {
       GET(steprec, (size_t)K * g.R * S); GET(trec, (size_t)K * (N - 1) * (7 * N + 1) * S);
       GET(tflag, (size_t)K * (N - 1) * S); GET(tscratch, (size_t)g.R * g.tgrid);
+      GET(pcap, (size_t)K * 2 * npk * PCAP * S + 1); GET(xsnap, (size_t)K * snap_count(gp.kick != 0) * 3 * N * S);
       GET(Jint, (size_t)S * 6 * N * 7 * N); GET(Eint, (size_t)S * 6 * N * 7 * N);
     }
 #undef GET
@@ -438,8 +443,9 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
       ctx->last_launches += 2;
       ctx->last_orbit_launches++;
       if (g.grad) {
+        if ((rc = timed(3, [&] { return kOps[g.N](g, (int)c, st); }))) return rc;
         if ((rc = timed(1, [&] { return kJac[g.N](g, (int)c, st); }))) return rc;
-        ctx->last_launches++;
+        ctx->last_launches += 3;
         ctx->last_jac_launches++;
       }
     }
@@ -478,7 +484,8 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
   for (auto& pr : prof) {
     float e = 0;
     cudaEventElapsedTime(&e, ctx->prof_events[pr.second], ctx->prof_events[pr.second + 1]);
-    (pr.first == 1 ? ctx->last_jac_ms : pr.first == 2 ? ctx->last_transit_ms : ctx->last_orbit_ms) += e;
+    (pr.first == 1 ? ctx->last_jac_ms : pr.first == 2 ? ctx->last_transit_ms
+                                      : pr.first == 3 ? ctx->last_ops_ms : ctx->last_orbit_ms) += e;
   }
   if (status_host) {
     std::fill(status_host, status_host + nsys, 0u);
@@ -610,7 +617,7 @@ int nbg_last_kernel_stats(nbg_context* ctx, int64_t* orbit_launches, int64_t* ja
 int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double* transit_ms, double* jacobian_ms) {
   if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
   if (total_ms) *total_ms = ctx->last_total_ms;
-  if (orbit_ms) *orbit_ms = ctx->last_orbit_ms;
+  if (orbit_ms) *orbit_ms = ctx->last_orbit_ms + ctx->last_ops_ms;
   if (transit_ms) *transit_ms = ctx->last_transit_ms;
   if (jacobian_ms) *jacobian_ms = ctx->last_jac_ms;
   return NBG_OK;

@@ -11,4 +11,5 @@ template int launch_orbit<NBG_N>(const GroupArgs&, int, cudaStream_t);
 template int launch_jac<NBG_N>(const GroupArgs&, int, cudaStream_t);
 template int launch_seed<NBG_N>(const GroupArgs&, cudaStream_t);
 template int launch_transit<NBG_N>(const GroupArgs&, int, cudaStream_t);
+template int launch_operators<NBG_N>(const GroupArgs&, int, cudaStream_t);
 }  // namespace nbg

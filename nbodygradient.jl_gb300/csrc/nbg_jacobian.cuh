@@ -16,7 +16,7 @@
 // 144 for the dense 12x12 block; the product is rounded differently from a
 // dense BLAS product, which the reference's BLAS leaves unspecified anyway.
 #pragma once
-#include "nbg_orbit.cuh"
+#include "nbg_operators.cuh"
 
 namespace nbg {
 

@@ -51,11 +51,14 @@ __global__ void __launch_bounds__(PROD_BS) orbit_chunk_kernel(GroupArgs g, int c
     const long long istep = k0 + kk;
     if (istep >= nst) break;
     if (g.grad) {
-      Rec rec{g.steprec + (size_t)kk * g.R * S + s, S};
-      if (istep == nst - 1) ahl21_step<N, true, true>(st, w, h, kick, rec);
-      else ahl21_step<N, true, false>(st, w, h, kick, rec);
+      // x, v only; the operators are built from the captures by the operator
+      // kernels.  The last step also computes dq/dt, the State's output.
+      Rec cap{g.pcap + (size_t)kk * 2 * g.npk * PCAP * S + s, S};
+      Rec xs{g.xsnap + (size_t)kk * snap_count(kick != 0) * 3 * N * S + s, S};
+      if (istep == nst - 1) ahl21_step<N, true, true>(st, w, h, kick, Rec{nullptr, 0}, cap, xs);
+      else ahl21_step<N, false, false>(st, w, h, kick, Rec{nullptr, 0}, cap, xs);
     } else {
-      ahl21_step<N, false, false>(st, w, h, kick, Rec{nullptr, 0});
+      ahl21_step<N, false, false>(st, w, h, kick, Rec{nullptr, 0}, Rec{nullptr, 0}, Rec{nullptr, 0});
     }
     const double t = t0 + (double)(istep + 1) * h;
     // detect_transits! (timing.jl:3-28).  The search itself (findtransit!) is
@@ -115,6 +118,11 @@ __global__ void __launch_bounds__(PROD_BS) orbit_chunk_kernel(GroupArgs g, int c
 // dt0 with its operator records and the adjoint row u^T = w^T S(dt0) that the
 // Jacobian consumer turns into dtdq0 (dtbvdq! row 1, timing.jl:155-171).
 // One lane per search, grid-stride over the queue.
+// The iterations take x, v only and the physical time derivative of g
+// (gdot_physical) where the reference builds the full gradient step to read
+// g's step derivative: both iterations stop at the same root of g to
+// rounding; the converged search's step keeps the reference's derivative,
+// which dtdq0 divides by.
 template <int N>
 __global__ void __launch_bounds__(TRANSIT_BS) transit_kernel(GroupArgs g, int chunk) {
   const int ntask = min(*g.task_count, g.task_cap);
@@ -148,9 +156,9 @@ __global__ void __launch_bounds__(TRANSIT_BS) transit_kernel(GroupArgs g, int ch
       tt2 = tt1;
       tt1 = dt0;
       wk = st;
-      ahl21_step<N, true, true>(wk, w, dt0, kick, Rec{nullptr, 0});
+      ahl21_step<N, false, false>(wk, w, dt0, kick, Rec{nullptr, 0}, Rec{nullptr, 0}, Rec{nullptr, 0});
       const double gs = gsky(wk, ti, ib);
-      const double gd = gdot(wk, ti, ib);
+      const double gd = gdot_physical(wk, ti, ib);
       const double dt = -gs / gd;
       kahan(dt0, stmp, dt);
       iter += 1;
@@ -160,7 +168,7 @@ __global__ void __launch_bounds__(TRANSIT_BS) transit_kernel(GroupArgs g, int ch
     if (g.grad) {
       wk = st;
       Rec rec{g.tscratch + tid, G};
-      ahl21_step<N, true, true>(wk, w, dt0, kick, rec);
+      ahl21_step<N, true, true>(wk, w, dt0, kick, rec, Rec{nullptr, 0}, Rec{nullptr, 0});
       double u[7 * N];
       for (int q = 0; q < 7 * N; q++) u[q] = 0.0;
       const double dvx = wk.v[3 * ib] - wk.v[3 * ti], dvy = wk.v[3 * ib + 1] - wk.v[3 * ti + 1];
@@ -181,6 +189,71 @@ __global__ void __launch_bounds__(TRANSIT_BS) transit_kernel(GroupArgs g, int ch
       g.tflag[(size_t)slot * S + s] = c;
     }
     g.tt[g.off_tt[g.sysidx[s]] + ib + (long long)N * c] = t + dt0;
+  }
+}
+
+
+// Kepler-pair records of one chunk: one lane per (step, pair slot, system),
+// consecutive lanes = consecutive systems, so a warp shares its pair.
+template <int N>
+__global__ void __launch_bounds__(OPS_BS) operator_pair_kernel(GroupArgs g, int chunk) {
+  const int S = g.S, np2 = 2 * g.npk;
+  const long long L = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (L >= (long long)g.K * np2 * S) return;
+  const int s = (int)(L % S);
+  const long long rest = L / S;
+  const int slot = (int)(rest % np2), kk = (int)(rest / np2);
+  if (g.sysidx[s] < 0) return;
+  if ((long long)chunk * g.K + kk >= g.nsteps[s]) return;
+  const uint64_t kick = g.kick;
+  Rec cap{g.pcap + (size_t)kk * np2 * PCAP * S + s, S};
+  Rec rec{g.steprec + (size_t)kk * g.R * S + s, S};
+  const int roff = (kick ? op_size(N) : 0) + slot * PREC + (slot >= g.npk ? op_size(N) : 0);
+  // A pair with G (m_i + m_j) == 0 keeps the jac_ij of the last pair of the
+  // step that had mass (ahl21.jl:713 returns before refilling it); zero at the
+  // start of the step (zero_out!, ahl21.jl:8).
+  int q = slot;
+  while (q >= 0 && cap.get(q * PCAP + 6 + 15) == 0.0) q--;
+  if (q < 0) {
+    for (int e = 0; e < PREC; e++) rec.put(roff + e, 0.0);
+    return;
+  }
+  int i, j;
+  pair_of_slot<N>(q, g.npk, kick, &i, &j);
+  const double mi = g.m[i * S + s], mj = g.m[j * S + s];
+  if (q < g.npk) pair_record_from_capture<true>(cap, q * PCAP, mi, mj, rec, roff);
+  else pair_record_from_capture<false>(cap, q * PCAP, mi, mj, rec, roff);
+}
+
+// Corrector (and kick) records of one chunk: one lane per (step, system).
+template <int N>
+__global__ void __launch_bounds__(OPS_BS) operator_phi_kernel(GroupArgs g, int chunk) {
+  const int S = g.S;
+  const long long L = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (L >= (long long)g.K * S) return;
+  const int s = (int)(L % S), kk = (int)(L / S);
+  if (g.sysidx[s] < 0) return;
+  if ((long long)chunk * g.K + kk >= g.nsteps[s]) return;
+  const uint64_t kick = g.kick;
+  const double h = g.h[s];
+  Rec xs{g.xsnap + (size_t)kk * snap_count(kick != 0) * 3 * N * S + s, S};
+  Rec rec{g.steprec + (size_t)kk * g.R * S + s, S};
+  Sys<N> st;
+  Work<N> w;
+  for (int q = 0; q < N; q++) st.m[q] = g.m[q * S + s];
+  for (int q = 0; q < 3 * N; q++) st.x[q] = xs.get(q), st.v[q] = st.xe[q] = st.ve[q] = 0.0;
+  phic<N, true>(st, w, h, kick);
+  phisalpha<N, true>(st, w, h, 2.0, kick);
+  const int off_phi = (kick ? op_size(N) : 0) + g.npk * PREC;
+  put_op(rec, off_phi, w.op, op_size(N));
+  if (kick) {
+    const double h6 = h / 6.0;
+    for (int q = 0; q < 3 * N; q++) st.x[q] = xs.get(3 * N + q);
+    kickfast<N, true>(st, w, h6, kick);
+    put_op(rec, 0, w.op, op_size(N));
+    for (int q = 0; q < 3 * N; q++) st.x[q] = xs.get(6 * N + q);
+    kickfast<N, true>(st, w, h6, kick);
+    put_op(rec, off_phi + op_size(N) + g.npk * PREC, w.op, op_size(N));
   }
 }
 
@@ -279,6 +352,15 @@ int launch_jac(const GroupArgs& g, int chunk, cudaStream_t st) {
 template <int N>
 int launch_transit(const GroupArgs& g, int chunk, cudaStream_t st) {
   transit_kernel<N><<<g.tgrid / TRANSIT_BS, TRANSIT_BS, 0, st>>>(g, chunk);
+  return 0;
+}
+
+template <int N>
+int launch_operators(const GroupArgs& g, int chunk, cudaStream_t st) {
+  long long lanes = (long long)g.K * 2 * g.npk * g.S;
+  if (lanes > 0) operator_pair_kernel<N><<<(unsigned)((lanes + OPS_BS - 1) / OPS_BS), OPS_BS, 0, st>>>(g, chunk);
+  lanes = (long long)g.K * g.S;
+  operator_phi_kernel<N><<<(unsigned)((lanes + OPS_BS - 1) / OPS_BS), OPS_BS, 0, st>>>(g, chunk);
   return 0;
 }
 

@@ -24,6 +24,15 @@ __host__ __device__ inline int step_record_size(int N, int npk, bool kick) {
 constexpr int PROD_BS = 32;     // orbit producer: one warp per block, spread over SMs
 constexpr int CONS_BS = 128;    // Jacobian consumer: four warps per block
 constexpr int TRANSIT_BS = 32;  // transit searches: one warp per block
+constexpr int OPS_BS = 128;     // operator kernels
+
+// Captured Kepler-pair parameters (producer -> operator kernel): x0[3], v0[3]
+// and the 22 values jac_delxv_gamma! returns (ahl21.jl:888-889).
+constexpr int PCAP = 28;
+// Position snapshots per step: [0] at the correctors, [1] at the first and
+// [2] at the second kick (kick groups only); 3N doubles each.
+__host__ __device__ inline int snap_count(bool kick) { return kick ? 3 : 1; }
+
 
 struct GroupArgs {
   int N, S, nsys, grad, K, R, npk;
@@ -54,11 +63,15 @@ struct GroupArgs {
   int task_cap;
   double* tscratch;  // [R][tgrid]: operator records of a search's final partial step
   int tgrid;         // threads of the transit kernel
+  // producer captures for the operator kernels
+  double* pcap;   // [K][2 npk][28][S]: Kepler-pair parameters
+  double* xsnap;  // [K][snaps][3N][S]: positions at the correctors (and kicks)
 };
 
 template <int N> int launch_orbit(const GroupArgs& g, int chunk, cudaStream_t st);
 template <int N> int launch_jac(const GroupArgs& g, int chunk, cudaStream_t st);
 template <int N> int launch_seed(const GroupArgs& g, cudaStream_t st);
 template <int N> int launch_transit(const GroupArgs& g, int chunk, cudaStream_t st);
+template <int N> int launch_operators(const GroupArgs& g, int chunk, cudaStream_t st);
 
 }  // namespace nbg

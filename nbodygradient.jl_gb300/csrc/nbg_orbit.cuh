@@ -377,17 +377,28 @@ __device__ void phisalpha(Sys<N>& s, Work<N>& w, double h, double alpha, uint64_
 // kepler_driftij_gamma! (ahl21.jl:706-760 with the block update of :31-42 on
 // dq/dt; ahl21_no_grad.jl:192-212 without Jacobian).
 template <int N, bool DRIFT_FIRST, bool GRADOPS, bool DQDT>
-__device__ void kepler_pair(Sys<N>& s, Work<N>& w, int i, int j, double h2, const Rec& rec, int roff) {
+__device__ void kepler_pair(Sys<N>& s, Work<N>& w, int i, int j, double h2, const Rec& rec, int roff,
+                            const Rec& cap, int coff) {
   double x0[3], v0[3];
   for (int k = 0; k < 3; k++) {
     x0[k] = s.x[3 * i + k] - s.x[3 * j + k];
     v0[k] = s.v[3 * i + k] - s.v[3 * j + k];
   }
   double gm = GNEWT * (s.m[i] + s.m[j]);
+  if (cap.p && gm == 0.0) cap.put(coff + 6 + 15, 0.0);  // k = 0 marks a pair that keeps the stale jac_ij
   if (gm != 0.0) {
     KepParams P;
     double delxv[6];
     kep_delxv<DRIFT_FIRST, GRADOPS>(x0, v0, gm, h2, delxv, P);
+    if (cap.p) {
+      for (int q = 0; q < 3; q++) {
+        cap.put(coff + q, x0[q]);
+        cap.put(coff + 3 + q, v0[q]);
+      }
+      const double pv[22] = {P.gamma, P.g0, P.g1, P.g2, P.g3, P.h1, P.h2, P.dfdt, P.fm1, P.gmh, P.dgdtm1,
+                             P.r0, P.r, P.r0inv, P.rinv, P.k, P.h, P.beta, P.betainv, P.eta, P.sqb, P.zeta};
+      for (int q = 0; q < 22; q++) cap.put(coff + 6 + q, pv[q]);
+    }
     double mijinv = 1.0 / (s.m[i] + s.m[j]);
     double mi = s.m[i] * mijinv, mj = s.m[j] * mijinv;
     if (GRADOPS) {
@@ -465,13 +476,18 @@ __device__ void kepler_pair(Sys<N>& s, Work<N>& w, int i, int j, double h2, cons
 //   GRADOPS: build the operators (needed for records and for dq/dt);
 //   DQDT:    compute dq/dt as the reference does;
 //   rec:     where the operator record goes (rec.p == nullptr: nowhere).
+//   cap, xs: where the Kepler-pair parameters and the position snapshots go
+//            for the operator kernel (p == nullptr: nowhere).
 template <int N, bool GRADOPS, bool DQDT>
-__device__ __noinline__ void ahl21_step(Sys<N>& s, Work<N>& w, double h, uint64_t kick, const Rec& rec) {
+__device__ __noinline__ void ahl21_step(Sys<N>& s, Work<N>& w, double h, uint64_t kick, const Rec& rec,
+                                        const Rec& cap, const Rec& xs) {
   const double h2 = 0.5 * h, h6 = h / 6.0;
   if (GRADOPS) reset_last(w);
   if (DQDT)
     for (int q = 0; q < 7 * N; q++) s.dqdt[q] = 0.0;
-  int roff = 0;
+  int roff = 0, slot = 0;
+  if (kick && xs.p)
+    for (int q = 0; q < 3 * N; q++) xs.put(3 * N + q, s.x[q]);
   if (kick) {
     kickfast<N, GRADOPS>(s, w, h6, kick);
     if (DQDT) dqdt_op(s, w, 6.0);
@@ -485,9 +501,12 @@ __device__ __noinline__ void ahl21_step(Sys<N>& s, Work<N>& w, double h, uint64_
   for (int i = 0; i < N - 1; i++)
     for (int j = i + 1; j < N; j++) {
       if ((kick >> pair_bit(i, j, N)) & 1) continue;
-      kepler_pair<N, true, GRADOPS, DQDT>(s, w, i, j, h2, rec, roff);
+      kepler_pair<N, true, GRADOPS, DQDT>(s, w, i, j, h2, rec, roff, cap, slot * PCAP);
       roff += PREC;
+      slot++;
     }
+  if (xs.p)
+    for (int q = 0; q < 3 * N; q++) xs.put(q, s.x[q]);
   phic<N, GRADOPS>(s, w, h, kick);
   phisalpha<N, GRADOPS>(s, w, h, 2.0, kick);
   if (DQDT) dqdt_op(s, w, 1.0);
@@ -496,8 +515,9 @@ __device__ __noinline__ void ahl21_step(Sys<N>& s, Work<N>& w, double h, uint64_
   for (int i = N - 2; i >= 0; i--)
     for (int j = N - 1; j > i; j--) {
       if ((kick >> pair_bit(i, j, N)) & 1) continue;
-      kepler_pair<N, false, GRADOPS, DQDT>(s, w, i, j, h2, rec, roff);
+      kepler_pair<N, false, GRADOPS, DQDT>(s, w, i, j, h2, rec, roff, cap, slot * PCAP);
       roff += PREC;
+      slot++;
     }
   drift(s, h2);
   if (DQDT)
@@ -505,6 +525,8 @@ __device__ __noinline__ void ahl21_step(Sys<N>& s, Work<N>& w, double h, uint64_
       for (int k = 0; k < 3; k++)
         s.dqdt[7 * b + k] = s.dqdt[7 * b + k] + (0.5 * s.v[3 * b + k] + h2 * s.dqdt[7 * b + 3 + k]);
   if (kick) {
+    if (xs.p)
+      for (int q = 0; q < 3 * N; q++) xs.put(6 * N + q, s.x[q]);
     kickfast<N, GRADOPS>(s, w, h6, kick);
     if (DQDT) dqdt_op(s, w, 6.0);
     if (GRADOPS) put_op(rec, roff, w.op, op_size(N));

@@ -197,7 +197,8 @@ def test_batch_matches_oracle():
     states, timings, hs, tms, grads = _batch_inputs(specs)
     gs = [s.copy() for s in states]
     status = nbg.integrate_transits_batch(gs, timings, hs, tms, True)
-    assert np.all(status == 0)
+    # a transit Newton search that stops at ITMAX is allowed (the reference continues silently)
+    assert np.all((status & ~np.uint32(nbg._lib.NBG_STATUS_NEWTON_ITMAX)) == 0)
     for q, (el, h, tmax, _) in enumerate(specs):
         x, v, jinit = states[q].x, states[q].v, states[q].jac_init
         so = O.OState(x, v, states[q].m, jac_init=jinit)
