@@ -130,6 +130,40 @@ int nbg_batch_integrate_transits_device(nbg_context* ctx, int nsys, const nbg_sy
                                         const double* jac_init, double* tt, double* dtdq0, double* dtdelements,
                                         int64_t* count, uint32_t* status);
 
+/*
+ * Allocation-free form of nbg_batch_integrate_transits_device (no
+ * counterpart in the reference): same arguments, same results, but the call
+ * allocates no device memory.  It is meant for callers that cannot let a
+ * library allocate while they run -- a sampler or pipeline that reserves the
+ * GPU's memory for itself and hands over only its own buffers, or a loop that
+ * must not pay the device-wide synchronisation of cudaMalloc / cudaFree when
+ * a larger batch arrives (the other entry points grow a per-context buffer
+ * cache that way).
+ *
+ * All working memory comes from one fixed array of NBG_NOALLOC_SCRATCH_BYTES
+ * in the library, per device.  A call whose working set does not fit even at
+ * one integration step per chunk, or that passes more than
+ * NBG_NOALLOC_MAX_SYSTEMS systems, is rejected with NBG_ENOMEM / NBG_EINVAL
+ * and a message naming the sizes; larger batches fit by shortening the
+ * chunk, at some speed.
+ *
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture on the device.  Every call on a device shares
+ * the one array and finds the previous call's contents in it (the call
+ * clears what must start at zero itself).  Calls that overlap on the GPU --
+ * from two threads, two contexts or two streams of the same device -- race
+ * on the array and corrupt each other's results: serialise them.  The call
+ * returns when its results are in the caller's arrays.
+ */
+#define NBG_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+#define NBG_NOALLOC_MAX_SYSTEMS 128
+int nbg_batch_integrate_transits_noalloc(nbg_context* ctx, int nsys, const nbg_system_desc* desc_host, double* t,
+                                         double* x, double* v, const double* m, double* xerror, double* verror,
+                                         double* jac_step, double* jac_error, double* dqdt, const uint8_t* pair,
+                                         const double* jac_init, double* tt, double* dtdq0, double* dtdelements,
+                                         int64_t* count, uint32_t* status);
+
 /* Tuning knobs of a context (0 keeps the current value).
  * chunk_steps: steps per producer/consumer chunk; overlap: run the orbit
  * producer and the Jacobian consumer on two streams. */

@@ -253,6 +253,22 @@ class Batch:
             vp("dtdq0"), vp("dtdelements"), vp("count"), __import__("ctypes").c_void_p(self.status.ctypes.data)))
         return self
 
+    def run_device_noalloc(self, dev_arrays, ctx=None):
+        """nbg_batch_integrate_transits_noalloc on device buffers: the same call
+        with every working buffer taken from the library's fixed scratch array
+        (at most NBG_NOALLOC_MAX_SYSTEMS systems); the library allocates no
+        device memory."""
+        import ctypes
+        ctx = ctx or default_context()
+        L = _lib.load()
+        d = dev_arrays
+        vp = lambda k: ctypes.c_void_p(d[k].data_ptr())
+        _lib.check(L.nbg_batch_integrate_transits_noalloc(
+            ctx.handle, self.nsys, self.descriptors(), vp("t"), vp("x"), vp("v"), vp("m"), vp("xerror"),
+            vp("verror"), vp("jac_step"), vp("jac_error"), vp("dqdt"), vp("pair"), vp("jac_init"), vp("tt"),
+            vp("dtdq0"), vp("dtdelements"), vp("count"), ctypes.c_void_p(self.status.ctypes.data)))
+        return self
+
 
 def integrate_transits_batch(states, timings, h, tmax, grad=True, ctx=None):
     """Integrate many (State, TransitTiming) pairs in one GPU plan; updates them in place."""

@@ -32,6 +32,7 @@ EXPORTS = (
     "nbg_integrate_transits", "nbg_batch_integrate_transits", "nbg_batch_integrate_transits_device",
     "nbg_set_tuning", "nbg_last_timing", "nbg_last_launch_count", "nbg_fp64_peak",
     "nbg_set_profiling", "nbg_last_kernel_stats", "nbg_set_orbit_lanes",
+    "nbg_batch_integrate_transits_noalloc",
 )
 
 
@@ -88,6 +89,7 @@ def load(build_if_missing=True):
                   _D, _I64, _U32]
     L.nbg_batch_integrate_transits.argtypes = batch_args
     L.nbg_batch_integrate_transits_device.argtypes = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc)] + [_VP] * 16
+    L.nbg_batch_integrate_transits_noalloc.argtypes = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc)] + [_VP] * 16
     L.nbg_set_tuning.argtypes = [_VP, ctypes.c_int, ctypes.c_int]
     L.nbg_last_timing.argtypes = [_VP, _D, _D, _D, _D]
     L.nbg_last_launch_count.argtypes = [_VP]

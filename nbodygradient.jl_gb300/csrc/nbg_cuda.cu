@@ -503,6 +503,311 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
 
 }  // namespace
 
+// ====================================================== allocation-free call
+//
+// nbg_batch_integrate_transits_noalloc runs the same kernels in the same
+// order as run_batch, but takes every device buffer from the fixed scratch
+// array of nbg_noalloc.cu (bump allocation, 256-byte aligned) and keeps its
+// host bookkeeping on the stack.  The steps per chunk (and the transit
+// kernel's thread count) shrink until the working set fits; neither changes
+// the arithmetic of any system.
+
+cudaError_t nbg_noalloc_scratch(int device, unsigned char** out);  // nbg_noalloc.cu
+
+namespace {
+
+struct ScratchArena {
+  unsigned char* base;  // nullptr: measure only
+  size_t used;
+  template <class T>
+  void take(T** out, size_t count) {
+    const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+    const size_t at = (used + 255) / 256 * 256;
+    used = at + bytes;
+    *out = base ? (T*)(base + at) : nullptr;
+  }
+};
+
+constexpr int kNaMax = NBG_NOALLOC_MAX_SYSTEMS;
+
+struct NoallocPlan {
+  SysOff off[kNaMax];
+  long long offtt[kNaMax], offdq[kNaMax], nsteps[kNaMax];
+  double hsig[kNaMax], t0[kNaMax], tout[kNaMax];
+  uint8_t pair[kNaMax * NBG_MAX_BODIES * NBG_MAX_BODIES];
+  int order[kNaMax];                 // systems by group, longest first within a group
+  int ngroups, gstart[kNaMax + 1];   // group q owns order[gstart[q] .. gstart[q+1])
+  int gN[kNaMax], ggrad[kNaMax];
+  unsigned long long gkick[kNaMax];
+  long long gmax[kNaMax];
+  GroupArgs g[kNaMax];
+};
+
+// Carves the device buffers of every group for chunk length K and transit
+// grid cap tcap; with a.base == nullptr it only measures.
+void noalloc_layout(NoallocPlan& P, ScratchArena& a, int nsys, int K, int tcap, SysOff** d_off,
+                    long long** d_offtt, long long** d_offdq, int** d_bad) {
+  a.take(d_off, (size_t)nsys);
+  a.take(d_offtt, (size_t)nsys);
+  a.take(d_offdq, (size_t)nsys);
+  a.take(d_bad, 1);
+  for (int q = 0; q < P.ngroups; q++) {
+    GroupArgs& g = P.g[q];
+    const int N = g.N, S = g.S;
+    g.K = K;
+    g.task_cap = K * (N - 1) * S;
+    g.tgrid = std::min(((g.task_cap + 31) / 32) * 32, tcap);
+    a.take(&g.x, 3 * N * S); a.take(&g.v, 3 * N * S); a.take(&g.xe, 3 * N * S); a.take(&g.ve, 3 * N * S);
+    a.take(&g.m, N * S); a.take(&g.dqdt, 7 * N * S); a.take(&g.gsave, N * S); a.take(&g.count, N * S);
+    a.take(&g.t0, S); a.take(&g.h, S); a.take(&g.hI, S); a.take(&g.nsteps, S); a.take(&g.ntt, S);
+    a.take(&g.ti, S); a.take(&g.sysidx, S); a.take(&g.status, S);
+    a.take(&g.task_f, (size_t)g.task_cap * (12 * N + 2)); a.take(&g.task_i, (size_t)g.task_cap * 3);
+    a.take(&g.task_count, 1);
+    if (g.grad) {
+      a.take(&g.steprec, (size_t)K * g.R * S); a.take(&g.trec, (size_t)K * (N - 1) * (7 * N + 1) * S);
+      a.take(&g.tflag, (size_t)K * (N - 1) * S); a.take(&g.tscratch, (size_t)g.R * g.tgrid);
+      a.take(&g.pcap, (size_t)K * 2 * g.npk * PCAP * S + 1);
+      a.take(&g.xsnap, (size_t)K * snap_count(g.kick != 0) * 3 * N * S);
+      a.take(&g.Jint, (size_t)S * 6 * N * 7 * N); a.take(&g.Eint, (size_t)S * 6 * N * 7 * N);
+    }
+  }
+}
+
+int run_batch_noalloc(nbg_context* ctx, NoallocPlan& P, int nsys, const nbg_system_desc* desc, double* d_t,
+                      double* d_x, double* d_v, const double* d_m, double* d_xe, double* d_ve, double* d_J,
+                      double* d_E, double* d_dqdt, const uint8_t* d_pair, const double* d_jinit, double* d_tt,
+                      double* d_dq0, double* d_dtdel, long long* d_count, uint32_t* status_host) {
+  cudaStream_t st = ctx->stream;
+  ctx->last_launches = 0;
+  ctx->last_orbit_ms = ctx->last_jac_ms = ctx->last_transit_ms = ctx->last_ops_ms = 0;
+  ctx->last_orbit_launches = ctx->last_jac_launches = 0;
+  // ---- offsets, steps, groups (host, no heap)
+  long long ax = 0, am = 0, aJ = 0, adq = 0, ap = 0, att = 0, adq0 = 0, acn = 0;
+  for (int s = 0; s < nsys; s++) {
+    const nbg_system_desc& d = desc[s];
+    if (d.n < NBG_MIN_BODIES || d.n > NBG_MAX_BODIES)
+      return set_error(NBG_EUNSUPPORTED, "system %d: n = %d outside the built range %d..%d", s, d.n, NBG_MIN_BODIES,
+                       NBG_MAX_BODIES);
+    if (d.ti < 0 || d.ti >= d.n) return set_error(NBG_EINVAL, "system %d: ti = %d not in 0..%d", s, d.ti, d.n - 1);
+    if (d.ntt < 1) return set_error(NBG_EINVAL, "system %d: ntt = %d < 1", s, d.ntt);
+    if (!(d.h != 0.0) || !std::isfinite(d.h) || !std::isfinite(d.tmax))
+      return set_error(NBG_EINVAL, "system %d: h = %g, tmax = %g", s, d.h, d.tmax);
+    const int n = d.n, M = 7 * n;
+    SysOff& o = P.off[s];
+    o.x = ax; o.m = am; o.J = aJ; o.dqdt = adq; o.pair = ap; o.tt = att; o.dq = adq0; o.cnt = acn;
+    o.n = n; o.ntt = d.ntt; o.grad = d.grad ? 1 : 0; o.pad = 0;
+    P.offtt[s] = att;
+    P.offdq[s] = adq0;
+    ax += 3 * n; am += n; aJ += (long long)M * M; adq += M; ap += (long long)n * n;
+    att += (long long)n * d.ntt; adq0 += (long long)n * d.ntt * 7 * n; acn += n;
+  }
+  // start times and pair flags steer the plan: bring them to the host
+  NBG_CUDA(cudaMemcpyAsync(P.t0, d_t, sizeof(double) * nsys, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(P.pair, d_pair, (size_t)ap, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaStreamSynchronize(st));
+  P.ngroups = 0;
+  int gof[kNaMax];
+  for (int s = 0; s < nsys; s++) {
+    const int n = desc[s].n;
+    P.nsteps[s] = steps_of(desc[s].h, desc[s].tmax);
+    P.hsig[s] = desc[s].h * check_step(P.t0[s], desc[s].tmax + P.t0[s]);
+    unsigned long long kick = 0;
+    for (int i = 0; i < n - 1; i++)
+      for (int j = i + 1; j < n; j++)
+        if (P.pair[P.off[s].pair + i + (long long)n * j]) kick |= 1ull << pair_bit(i, j, n);
+    int q = 0;
+    while (q < P.ngroups && !(P.gN[q] == n && P.ggrad[q] == P.off[s].grad && P.gkick[q] == kick)) q++;
+    if (q == P.ngroups) {
+      P.gN[q] = n; P.ggrad[q] = P.off[s].grad; P.gkick[q] = kick; P.gmax[q] = 0;
+      P.ngroups++;
+    }
+    gof[s] = q;
+    P.gmax[q] = std::max(P.gmax[q], P.nsteps[s]);
+  }
+  // order: by group, then by steps (longest first, stable)
+  int pos = 0;
+  for (int q = 0; q < P.ngroups; q++) {
+    P.gstart[q] = pos;
+    for (int s = 0; s < nsys; s++)
+      if (gof[s] == q) {
+        int k = pos++;
+        while (k > P.gstart[q] && P.nsteps[P.order[k - 1]] < P.nsteps[s]) {
+          P.order[k] = P.order[k - 1];
+          k--;
+        }
+        P.order[k] = s;
+      }
+  }
+  P.gstart[P.ngroups] = pos;
+  for (int q = 0; q < P.ngroups; q++) {
+    GroupArgs& g = P.g[q];
+    memset(&g, 0, sizeof(g));
+    const int N = P.gN[q], nsg = P.gstart[q + 1] - P.gstart[q];
+    g.N = N; g.S = ((nsg + 31) / 32) * 32; g.nsys = nsg; g.grad = P.ggrad[q]; g.kick = P.gkick[q];
+    if (ctx->orbit_spw > 0) {
+      g.spw = ctx->orbit_spw;
+    } else {
+      int target = std::max(1, 2 * ctx->sm_count);
+      int want = (nsg + target - 1) / target, spw = 1;
+      while (spw < want && spw < 32) spw *= 2;
+      g.spw = spw;
+    }
+    int npk = 0;
+    for (int i = 0; i < N - 1; i++)
+      for (int j = i + 1; j < N; j++)
+        if (!((g.kick >> pair_bit(i, j, N)) & 1)) npk++;
+    g.npk = npk;
+    g.R = step_record_size(N, npk, g.kick != 0);
+  }
+  // ---- fit the working set: longest chunk first, then the widest transit grid
+  SysOff* d_off;
+  long long *d_offtt, *d_offdq;
+  int* d_bad;
+  const size_t limit = (size_t)NBG_NOALLOC_SCRATCH_BYTES;
+  int K = 0, tcap = 0;
+  size_t need_min = 0;
+  for (int k = std::max(1, ctx->chunk_steps); k >= 1 && !K; k = (k > 1 ? k / 2 : 0))
+    for (int tc = 1024; tc >= 32 && !K; tc /= 2) {
+      ScratchArena a{nullptr, 0};
+      noalloc_layout(P, a, nsys, k, tc, &d_off, &d_offtt, &d_offdq, &d_bad);
+      need_min = a.used;
+      if (a.used <= limit) { K = k; tcap = tc; }
+    }
+  if (!K)
+    return set_error(NBG_ENOMEM,
+                     "nbg_batch_integrate_transits_noalloc: these %d systems need %zu bytes of device scratch even "
+                     "at one step per chunk; the fixed scratch holds %zu bytes (NBG_NOALLOC_SCRATCH_BYTES)",
+                     nsys, need_min, limit);
+  unsigned char* base = nullptr;
+  {
+    cudaError_t e = nbg_noalloc_scratch(ctx->device, &base);
+    if (e != cudaSuccess)
+      return set_error(NBG_ECUDA, "cudaGetSymbolAddress of the no-allocation scratch on device %d: %s", ctx->device,
+                       cudaGetErrorString(e));
+  }
+  {
+    ScratchArena a{base, 0};
+    noalloc_layout(P, a, nsys, K, tcap, &d_off, &d_offtt, &d_offdq, &d_bad);
+  }
+  NBG_CUDA(cudaMemcpyAsync(d_off, P.off, sizeof(SysOff) * nsys, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_offtt, P.offtt, sizeof(long long) * nsys, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_offdq, P.offdq, sizeof(long long) * nsys, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(int), st));
+  // ---- per-group state: scalars through one stack staging area per group
+  for (int q = 0; q < P.ngroups; q++) {
+    GroupArgs& g = P.g[q];
+    const int N = g.N, S = g.S;
+    g.tt = d_tt; g.off_tt = d_offtt; g.dtdq0 = d_dq0; g.off_dq = d_offdq;
+    int sidx[kNaMax], vntt[kNaMax], vti[kNaMax];
+    double vt0[kNaMax], vh[kNaMax], vhI[kNaMax];
+    long long vns[kNaMax];
+    for (int r = 0; r < S; r++) {
+      sidx[r] = -1; vntt[r] = 1; vti[r] = 0; vt0[r] = vh[r] = vhI[r] = 0.0; vns[r] = 0;
+    }
+    for (int r = 0; r < g.nsys; r++) {
+      const int s = P.order[P.gstart[q] + r];
+      sidx[r] = s; vntt[r] = desc[s].ntt; vti[r] = desc[s].ti;
+      vt0[r] = P.t0[s]; vh[r] = P.hsig[s]; vhI[r] = desc[s].h; vns[r] = P.nsteps[s];
+    }
+    NBG_CUDA(cudaMemcpyAsync(g.sysidx, sidx, sizeof(int) * S, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(g.ntt, vntt, sizeof(int) * S, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(g.ti, vti, sizeof(int) * S, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(g.t0, vt0, sizeof(double) * S, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(g.h, vh, sizeof(double) * S, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(g.hI, vhI, sizeof(double) * S, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(g.nsteps, vns, sizeof(long long) * S, cudaMemcpyHostToDevice, st));
+    NBG_CUDA(cudaMemsetAsync(g.status, 0, sizeof(unsigned) * S, st));
+    NBG_CUDA(cudaStreamSynchronize(st));  // the staging arrays go out of scope
+    const int pb = (S + 127) / 128;
+    pack_state_kernel<<<pb, 128, 0, st>>>(N, S, g.sysidx, d_off, d_x, d_v, d_xe, d_ve, d_m, d_dqdt, d_count, g.x,
+                                          g.v, g.xe, g.ve, g.m, g.dqdt, g.count);
+    ctx->last_launches++;
+    if (g.grad) {
+      const long long tot = (long long)S * 49 * N * N;
+      pack_jac_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(N, S, g.sysidx, d_off, d_J, d_E, g.Jint, g.Eint,
+                                                                     d_bad);
+      ctx->last_launches++;
+    }
+  }
+  NBG_CUDA(cudaGetLastError());
+  int bad = 0;
+  NBG_CUDA(cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaStreamSynchronize(st));
+  if (bad)
+    return set_error(NBG_EUNSUPPORTED,
+                     "jac_step mass rows must be unit rows with zero jac_error (true for every State the reference "
+                     "builds and integrates)");
+  for (int q = 0; q < P.ngroups; q++) {
+    kSeed[P.g[q].N](P.g[q], st);
+    ctx->last_launches++;
+  }
+  // ---- chunk loop
+  long long max_steps = 0;
+  for (int q = 0; q < P.ngroups; q++) max_steps = std::max(max_steps, P.gmax[q]);
+  const long long nchunks = (max_steps + K - 1) / K;
+  int rc;
+  NBG_CUDA(cudaEventRecord(ctx->ev0, st));
+  for (long long c = 0; c < nchunks; c++) {
+    for (int q = 0; q < P.ngroups; q++) {
+      const GroupArgs& g = P.g[q];
+      if (c * K >= P.gmax[q]) continue;
+      NBG_CUDA(cudaMemsetAsync(g.task_count, 0, sizeof(int), st));
+      if ((rc = kOrbit[g.N](g, (int)c, st))) return rc;
+      if ((rc = kTransit[g.N](g, (int)c, st))) return rc;
+      ctx->last_launches += 2;
+      ctx->last_orbit_launches++;
+      if (g.grad) {
+        if ((rc = kOps[g.N](g, (int)c, st))) return rc;
+        if ((rc = kJac[g.N](g, (int)c, st))) return rc;
+        ctx->last_launches += 3;
+        ctx->last_jac_launches++;
+      }
+    }
+  }
+  NBG_CUDA(cudaGetLastError());
+  NBG_CUDA(cudaEventRecord(ctx->ev1, st));
+  // ---- outputs
+  for (int q = 0; q < P.ngroups; q++) {
+    const GroupArgs& g = P.g[q];
+    const int pb = (g.S + 127) / 128;
+    unpack_state_kernel<<<pb, 128, 0, st>>>(g.N, g.S, g.grad, g.sysidx, d_off, d_x, d_v, d_xe, d_ve, d_dqdt, d_count,
+                                            g.x, g.v, g.xe, g.ve, g.dqdt, g.count);
+    ctx->last_launches++;
+    if (g.grad) {
+      const long long tot = (long long)g.S * 42 * g.N * g.N;
+      unpack_jac_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(g.N, g.S, g.sysidx, d_off, d_J, d_E, g.Jint,
+                                                                       g.Eint);
+      ctx->last_launches++;
+    }
+  }
+  {
+    dim3 grid(8, nsys, 1);
+    dtdelements_kernel<<<grid, 256, 0, st>>>(nsys, d_off, d_dq0, d_jinit, d_dtdel, d_count);
+    ctx->last_launches++;
+  }
+  // s.t = t0 + nsteps * h (Transits.jl:161 at the last step)
+  for (int s = 0; s < nsys; s++)
+    P.tout[s] = P.nsteps[s] > 0 ? P.t0[s] + (double)P.nsteps[s] * P.hsig[s] : P.t0[s];
+  NBG_CUDA(cudaMemcpyAsync(d_t, P.tout, sizeof(double) * nsys, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaStreamSynchronize(st));
+  NBG_CUDA(cudaGetLastError());
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  ctx->last_total_ms = ms;
+  if (status_host) {
+    std::fill(status_host, status_host + nsys, 0u);
+    for (int q = 0; q < P.ngroups; q++) {
+      const GroupArgs& g = P.g[q];
+      unsigned sv[kNaMax];
+      NBG_CUDA(cudaMemcpy(sv, g.status, sizeof(unsigned) * g.S, cudaMemcpyDeviceToHost));
+      for (int r = 0; r < g.nsys; r++) status_host[P.order[P.gstart[q] + r]] = sv[r];
+    }
+  }
+  return NBG_OK;
+}
+
+}  // namespace
+
 // FP64 FMA throughput probe: CHAINS independent FMA chains per thread, full
 // warps, several blocks per SM.  Every index stays inside the grid-sized
 // output buffer.
@@ -764,6 +1069,22 @@ int nbg_batch_integrate_transits_device(nbg_context* ctx, int nsys, const nbg_sy
   NBG_CUDA(cudaMemcpy(ph.data(), pair, ap, cudaMemcpyDeviceToHost));
   return run_batch(ctx, nsys, desc, th.data(), ph.data(), t, x, v, m, xerror, verror, jac_step, jac_error, dqdt,
                    jac_init, tt, dtdq0, dtdelements, (long long*)count, status);
+}
+
+int nbg_batch_integrate_transits_noalloc(nbg_context* ctx, int nsys, const nbg_system_desc* desc, double* t,
+                                         double* x, double* v, const double* m, double* xerror, double* verror,
+                                         double* jac_step, double* jac_error, double* dqdt, const uint8_t* pair,
+                                         const double* jac_init, double* tt, double* dtdq0, double* dtdelements,
+                                         int64_t* count, uint32_t* status) {
+  if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
+  if (!desc) return set_error(NBG_EINVAL, "desc is NULL");
+  if (nsys <= 0 || nsys > NBG_NOALLOC_MAX_SYSTEMS)
+    return set_error(NBG_EINVAL, "nbg_batch_integrate_transits_noalloc: nsys = %d not in 1..%d (NBG_NOALLOC_MAX_SYSTEMS)",
+                     nsys, NBG_NOALLOC_MAX_SYSTEMS);
+  NBG_CUDA(cudaSetDevice(ctx->device));
+  NoallocPlan plan;
+  return run_batch_noalloc(ctx, plan, nsys, desc, t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair,
+                           jac_init, tt, dtdq0, dtdelements, (long long*)count, status);
 }
 
 }  // extern "C"
