@@ -259,6 +259,7 @@ def main():
     ap.add_argument("--nsys", type=int, default=None)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--chunk", type=int, default=0)
+    ap.add_argument("--serial", action="store_true", help="one stream: no producer/consumer overlap")
     ap.add_argument("--spw", type=int, default=0, help="orbit producer systems per warp (0 = automatic)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=8.0)
@@ -283,8 +284,8 @@ def main():
     import torch
     torch.cuda.set_device(local_rank)
     ctx = nbg.Context(local_rank)
-    if args.chunk:
-        ctx.set_tuning(chunk_steps=args.chunk)
+    if args.chunk or args.serial:
+        ctx.set_tuning(chunk_steps=args.chunk, overlap=0 if args.serial else -1)
     if args.spw:
         ctx.set_orbit_lanes(args.spw)
     states, timings, hs, tms, nsteps = build_workload(nbg, args.workload, args.nsys, replica_seed(args.seed, rank))
@@ -366,7 +367,8 @@ def main():
             "config": {"workload": args.workload, "nsys": len(states), "system_steps_per_pass": total_ss,
                        "grad": True, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "working set larger than L2 (operator records + jac_step)",
-                       "chunk_steps": args.chunk or 16, "orbit_systems_per_warp": args.spw or "auto"},
+                       "chunk_steps": args.chunk or 16, "orbit_systems_per_warp": args.spw or "auto",
+                       "streams": 1 if args.serial else 2},
             "e2e": {"value": e2e_val, "unit": "system-steps/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.mean(e2e_ms)) if e2e_ms else None},
             "gpu_launches": int(launches),

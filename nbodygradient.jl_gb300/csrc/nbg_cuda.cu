@@ -178,7 +178,7 @@ struct nbg_context {
   cudaStream_t stream = nullptr;
   std::map<std::string, Buf> pool;
   int chunk_steps = 16;
-  int overlap = 0;
+  int overlap = 1;  // orbit producer on its own stream, one chunk ahead of the rest
   int orbit_spw = 0;  // 0: automatic
   int sm_count = 0;
   double last_total_ms = 0, last_orbit_ms = 0, last_jac_ms = 0, last_transit_ms = 0, last_ops_ms = 0;
@@ -186,6 +186,20 @@ struct nbg_context {
   int profile = 0;
   std::vector<cudaEvent_t> prof_events;  // pairs around each timed launch
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaStream_t stream_w = nullptr;       // operator / Jacobian stream (overlap mode)
+  cudaStream_t stream_t = nullptr;       // transit-search stream (overlap mode)
+  std::vector<cudaEvent_t> sync_events;  // cross-stream ordering, no timing
+
+  int sync_event(size_t i, cudaEvent_t* out) {
+    while (sync_events.size() <= i) {
+      cudaEvent_t e;
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+        return set_error(NBG_ECUDA, "cudaEventCreateWithFlags failed");
+      sync_events.push_back(e);
+    }
+    *out = sync_events[i];
+    return NBG_OK;
+  }
 
   int event(size_t i, cudaEvent_t* out) {
     while (prof_events.size() <= i) {
@@ -319,6 +333,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
   const int K = std::max(1, ctx->chunk_steps);
   // ---- per-group device state
   std::vector<GroupArgs> gargs;
+  std::vector<GroupArgs> ghalf;  // the same groups on the second half of the per-chunk buffers
   int* d_bad;
   if ((rc = ctx->get("bad", 1, &d_bad))) return rc;
   NBG_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(int), st));
@@ -357,12 +372,18 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     GET(dqdt, 7 * N * S); GET(gsave, N * S); GET(count, N * S); GET(t0, S); GET(h, S); GET(hI, S);
     GET(nsteps, S); GET(ntt, S); GET(ti, S); GET(sysidx, S); GET(status, S);
     g.task_cap = K * (N - 1) * S;
-    GET(task_f, (size_t)g.task_cap * (12 * N + 2)); GET(task_i, (size_t)g.task_cap * 3); GET(task_count, 1);
+    // Per-chunk buffers (the transit queue, the captures and the records) are
+    // double-buffered in overlap mode: chunk c uses half c % 2.
+    const size_t nf = (size_t)g.task_cap * (12 * N + 2), ni = (size_t)g.task_cap * 3;
+    const size_t nrec = (size_t)K * g.R * S, ntrec = (size_t)K * (N - 1) * (7 * N + 1) * S;
+    const size_t nflag = (size_t)K * (N - 1) * S, ncap = (size_t)K * 2 * npk * PCAP * S + 1;
+    const size_t nsnap = (size_t)K * snap_count(gp.kick != 0) * 3 * N * S;
+    const int nb = ctx->overlap ? 2 : 1;
+    GET(task_f, nb * nf); GET(task_i, nb * ni); GET(task_count, nb);
     g.tgrid = std::min(((g.task_cap + 31) / 32) * 32, std::max(1, ctx->sm_count) * 4 * 32);
     if (gp.grad) {
-      GET(steprec, (size_t)K * g.R * S); GET(trec, (size_t)K * (N - 1) * (7 * N + 1) * S);
-      GET(tflag, (size_t)K * (N - 1) * S); GET(tscratch, (size_t)g.R * g.tgrid);
-      GET(pcap, (size_t)K * 2 * npk * PCAP * S + 1); GET(xsnap, (size_t)K * snap_count(gp.kick != 0) * 3 * N * S);
+      GET(steprec, nb * nrec); GET(trec, nb * ntrec); GET(tflag, nb * nflag); GET(tscratch, (size_t)g.R * g.tgrid);
+      GET(pcap, nb * ncap); GET(xsnap, nb * nsnap);
       GET(Jint, (size_t)S * 6 * N * 7 * N); GET(Eint, (size_t)S * 6 * N * 7 * N);
     }
 #undef GET
@@ -397,6 +418,12 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
       ctx->last_launches++;
     }
     gargs.push_back(g);
+    {
+      GroupArgs h1 = g;
+      h1.task_f += nf; h1.task_i += ni; h1.task_count += 1;
+      if (gp.grad) { h1.steprec += nrec; h1.trec += ntrec; h1.tflag += nflag; h1.pcap += ncap; h1.xsnap += nsnap; }
+      ghalf.push_back(h1);
+    }
     gmaxsteps.push_back(gp.max_steps);
     gi++;
   }
@@ -431,24 +458,93 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     nev += 2;
     return r;
   };
+  // the same on another stream: the event pair brackets the launch on the
+  // stream it is launched on
+  auto timed_on = [&](cudaStream_t s2, int kind, auto&& launch) -> int {
+    if (!ctx->profile) return launch();
+    cudaEvent_t a, b;
+    int r;
+    if ((r = ctx->event(nev, &a)) || (r = ctx->event(nev + 1, &b))) return r;
+    cudaEventRecord(a, s2);
+    r = launch();
+    cudaEventRecord(b, s2);
+    prof.emplace_back(kind, nev);
+    nev += 2;
+    return r;
+  };
   ctx->last_orbit_launches = ctx->last_jac_launches = 0;
   NBG_CUDA(cudaEventRecord(ctx->ev0, st));
-  for (long long c = 0; c < nchunks; c++) {
-    for (size_t q = 0; q < gargs.size(); q++) {
-      const GroupArgs& g = gargs[q];
-      if (c * K >= gmaxsteps[q]) continue;
-      NBG_CUDA(cudaMemsetAsync(g.task_count, 0, sizeof(int), st));
-      if ((rc = timed(0, [&] { return kOrbit[g.N](g, (int)c, st); }))) return rc;
-      if ((rc = timed(2, [&] { return kTransit[g.N](g, (int)c, st); }))) return rc;
-      ctx->last_launches += 2;
-      ctx->last_orbit_launches++;
-      if (g.grad) {
-        if ((rc = timed(3, [&] { return kOps[g.N](g, (int)c, st); }))) return rc;
-        if ((rc = timed(1, [&] { return kJac[g.N](g, (int)c, st); }))) return rc;
-        ctx->last_launches += 3;
-        ctx->last_jac_launches++;
+  if (!ctx->overlap) {
+    for (long long c = 0; c < nchunks; c++) {
+      for (size_t q = 0; q < gargs.size(); q++) {
+        const GroupArgs& g = gargs[q];
+        if (c * K >= gmaxsteps[q]) continue;
+        NBG_CUDA(cudaMemsetAsync(g.task_count, 0, sizeof(int), st));
+        if ((rc = timed(0, [&] { return kOrbit[g.N](g, (int)c, st); }))) return rc;
+        if ((rc = timed(2, [&] { return kTransit[g.N](g, (int)c, st); }))) return rc;
+        ctx->last_launches += 2;
+        ctx->last_orbit_launches++;
+        if (g.grad) {
+          if ((rc = timed(3, [&] { return kOps[g.N](g, (int)c, st); }))) return rc;
+          if ((rc = timed(1, [&] { return kJac[g.N](g, (int)c, st); }))) return rc;
+          ctx->last_launches += 3;
+          ctx->last_jac_launches++;
+        }
       }
     }
+  } else {
+    // Three streams.  st runs the orbit producer, chunk after chunk; once
+    // the producer has finished chunk c, stt runs chunk c's transit searches
+    // while sw runs its operator kernels, and then (after the searches) its
+    // Jacobian consumer.  Chunk c + 2 reuses chunk c's buffer half, so the
+    // producer waits for chunk c's consumer before it starts chunk c + 2.
+    // The producer thus runs one chunk ahead, and the latency-bound producer
+    // and search warps share the SMs with the throughput-bound operator and
+    // Jacobian kernels.
+    if (!ctx->stream_w) NBG_CUDA(cudaStreamCreateWithFlags(&ctx->stream_w, cudaStreamNonBlocking));
+    if (!ctx->stream_t) NBG_CUDA(cudaStreamCreateWithFlags(&ctx->stream_t, cudaStreamNonBlocking));
+    cudaStream_t sw = ctx->stream_w, stt = ctx->stream_t;
+    cudaEvent_t evs, evt_join;
+    if ((rc = ctx->sync_event(0, &evs))) return rc;
+    NBG_CUDA(cudaEventRecord(evs, st));
+    NBG_CUDA(cudaStreamWaitEvent(sw, evs, 0));  // sw and stt start after the packing on st
+    NBG_CUDA(cudaStreamWaitEvent(stt, evs, 0));
+    for (long long c = 0; c < nchunks; c++) {
+      for (size_t q = 0; q < gargs.size(); q++) {
+        if (c * K >= gmaxsteps[q]) continue;
+        const int par = (int)(c & 1);
+        const GroupArgs& g = par ? ghalf[q] : gargs[q];
+        cudaEvent_t ev_orb, ev_done, ev_tr;
+        if ((rc = ctx->sync_event(2 + 6 * q + par, &ev_orb)) || (rc = ctx->sync_event(4 + 6 * q + par, &ev_done)) ||
+            (rc = ctx->sync_event(6 + 6 * q + par, &ev_tr)))
+          return rc;
+        if (c >= 2) NBG_CUDA(cudaStreamWaitEvent(st, ev_done, 0));
+        NBG_CUDA(cudaMemsetAsync(g.task_count, 0, sizeof(int), st));
+        if ((rc = timed(0, [&] { return kOrbit[g.N](g, (int)c, st); }))) return rc;
+        NBG_CUDA(cudaEventRecord(ev_orb, st));
+        NBG_CUDA(cudaStreamWaitEvent(stt, ev_orb, 0));
+        NBG_CUDA(cudaStreamWaitEvent(sw, ev_orb, 0));
+        if ((rc = timed_on(stt, 2, [&] { return kTransit[g.N](g, (int)c, stt); }))) return rc;
+        NBG_CUDA(cudaEventRecord(ev_tr, stt));
+        ctx->last_launches += 2;
+        ctx->last_orbit_launches++;
+        if (g.grad) {
+          if ((rc = timed_on(sw, 3, [&] { return kOps[g.N](g, (int)c, sw); }))) return rc;
+          NBG_CUDA(cudaStreamWaitEvent(sw, ev_tr, 0));
+          if ((rc = timed_on(sw, 1, [&] { return kJac[g.N](g, (int)c, sw); }))) return rc;
+          ctx->last_launches += 3;
+          ctx->last_jac_launches++;
+        } else {
+          NBG_CUDA(cudaStreamWaitEvent(sw, ev_tr, 0));
+        }
+        NBG_CUDA(cudaEventRecord(ev_done, sw));
+      }
+    }
+    if ((rc = ctx->sync_event(1, &evt_join))) return rc;
+    NBG_CUDA(cudaEventRecord(evs, sw));
+    NBG_CUDA(cudaEventRecord(evt_join, stt));
+    NBG_CUDA(cudaStreamWaitEvent(st, evs, 0));  // join: everything after runs on st
+    NBG_CUDA(cudaStreamWaitEvent(st, evt_join, 0));
   }
   NBG_CUDA(cudaGetLastError());
   NBG_CUDA(cudaEventRecord(ctx->ev1, st));
@@ -885,6 +981,12 @@ int nbg_destroy(nbg_context* ctx) {
   cudaEventDestroy(ctx->ev0);
   cudaEventDestroy(ctx->ev1);
   for (auto e : ctx->prof_events) cudaEventDestroy(e);
+  for (auto e : ctx->sync_events) cudaEventDestroy(e);
+  for (cudaStream_t s2 : {ctx->stream_w, ctx->stream_t})
+    if (s2) {
+      cudaStreamSynchronize(s2);
+      cudaStreamDestroy(s2);
+    }
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return NBG_OK;
