@@ -260,6 +260,8 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--serial", action="store_true", help="one stream: no producer/consumer overlap")
+    ap.add_argument("--kernel-timing", default="timed", choices=["timed", "separate"],
+                    help="CUDA-event pairs around each kernel inside the timed steps, or in one extra pass")
     ap.add_argument("--spw", type=int, default=0, help="orbit producer systems per warp (0 = automatic)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=8.0)
@@ -286,6 +288,7 @@ def main():
     ctx = nbg.Context(local_rank)
     if args.chunk or args.serial:
         ctx.set_tuning(chunk_steps=args.chunk, overlap=0 if args.serial else -1)
+    chunk = args.chunk or 32  # the library's default chunk length
     if args.spw:
         ctx.set_orbit_lanes(args.spw)
     states, timings, hs, tms, nsteps = build_workload(nbg, args.workload, args.nsys, replica_seed(args.seed, rank))
@@ -311,6 +314,11 @@ def main():
     clk = ClockSampler(local_rank)
     clk.start()
     launches = 0
+    # per-kernel CUDA-event pairs on each kernel's own stream, summed over the
+    # timed steps: the roofline's kernel durations come from the timed region
+    ctx.set_profiling(args.kernel_timing == "timed")
+    kt = np.zeros(4)
+    kn = np.zeros(2, dtype=np.int64)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -318,8 +326,11 @@ def main():
     for _ in range(args.steps):
         step()
         launches += ctx.last_launch_count()
+        kt += np.array(ctx.last_timing())
+        kn += np.array(ctx.last_kernel_stats(), dtype=np.int64)
     e1.record()
     torch.cuda.synchronize()
+    ctx.set_profiling(False)
     clocks = clk.stop()
     ms = reduce_max_ms(e0.elapsed_time(e1) / args.steps, dist)
     value = aggregate_value(total_ss, world, ms)
@@ -344,20 +355,28 @@ def main():
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_val = total_ss * world / (np.mean(e2e_ms) * 1e-3) if e2e_ms else None
 
-    # roofline of the dominant kernel (Jacobian consumer) from one profiled pass
-    ctx.set_profiling(True)
-    step()
-    ctx.set_profiling(False)
-    total_ms, orbit_ms, transit_ms, jac_ms = ctx.last_timing()
-    n_orbit, n_jac = ctx.last_kernel_stats()
+    if args.kernel_timing == "separate":
+        # one more pass with the event pairs, after the timed region
+        ctx.set_profiling(True)
+        step()
+        ctx.set_profiling(False)
+        kt = np.array(ctx.last_timing()) * args.steps
+        kn = np.array(ctx.last_kernel_stats(), dtype=np.int64) * args.steps
+    # roofline of the Jacobian consumer, averaged over the timed steps
+    total_ms, orbit_ms, transit_ms, jac_ms = kt / args.steps
+    n_orbit, n_jac = (int(v) // args.steps for v in kn)
     flops = sum(flops_per_system_step(s.n) * ns for s, ns in zip(states, nsteps))
     peak = ctx.fp64_peak_tflops()
     achieved = flops / (jac_ms * 1e-3) / 1e12 if jac_ms > 0 else None
+    # DRAM bytes per launch: ncu's per-system-step figure for this kernel and
+    # workload times the system-steps one launch processes (chunk x systems)
     traffic = None
     prof_json = os.path.join(ROOT, "profiles", "jacobian_consumer_%s.json" % args.workload)
     if os.path.exists(prof_json):
         with open(prof_json) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
+            per_unit = json.load(f).get("dram_bytes_per_system_step")
+        if per_unit:
+            traffic = per_unit * chunk * len(states)
 
     if rank == 0:
         line = {
@@ -367,8 +386,8 @@ def main():
             "config": {"workload": args.workload, "nsys": len(states), "system_steps_per_pass": total_ss,
                        "grad": True, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "working set larger than L2 (operator records + jac_step)",
-                       "chunk_steps": args.chunk or 16, "orbit_systems_per_warp": args.spw or "auto",
-                       "streams": 1 if args.serial else 2},
+                       "chunk_steps": chunk, "orbit_systems_per_warp": args.spw or "auto",
+                       "streams": 1 if args.serial else 3},
             "e2e": {"value": e2e_val, "unit": "system-steps/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.mean(e2e_ms)) if e2e_ms else None},
             "gpu_launches": int(launches),

@@ -164,9 +164,13 @@ int nbg_batch_integrate_transits_noalloc(nbg_context* ctx, int nsys, const nbg_s
                                          const double* jac_init, double* tt, double* dtdq0, double* dtdelements,
                                          int64_t* count, uint32_t* status);
 
-/* Tuning knobs of a context (0 keeps the current value).
- * chunk_steps: steps per producer/consumer chunk; overlap: run the orbit
- * producer and the Jacobian consumer on two streams. */
+/* Tuning knobs of a context.  Results do not depend on them.
+ * chunk_steps: integration steps per producer/consumer chunk (default 32;
+ *   0 keeps the current value);
+ * overlap: 1 (default) runs the orbit producer on its own stream one chunk
+ *   ahead of the transit searches, operator kernels and Jacobian consumer
+ *   (two more streams of the context); 0 runs everything on one stream;
+ *   a negative value keeps the current setting. */
 int nbg_set_tuning(nbg_context* ctx, int chunk_steps, int overlap);
 
 /* Device time (ms) of the last batched call's integration, measured with

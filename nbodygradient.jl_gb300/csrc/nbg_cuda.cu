@@ -177,7 +177,7 @@ struct nbg_context {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::map<std::string, Buf> pool;
-  int chunk_steps = 16;
+  int chunk_steps = 32;
   int overlap = 1;  // orbit producer on its own stream, one chunk ahead of the rest
   int orbit_spw = 0;  // 0: automatic
   int sm_count = 0;
@@ -348,11 +348,16 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     GroupArgs g;
     memset(&g, 0, sizeof(g));
     g.N = N; g.S = S; g.nsys = nsg; g.grad = gp.grad; g.K = K; g.kick = gp.kick;
-    // Orbit producer lanes per warp: a warp's FP64 instruction costs the same
-    // issue slot at any lane count, but the producer is latency bound, so a
-    // small batch is spread over about two warps per SM.
+    // Orbit producer lanes per warp.  A warp's FP64 instruction occupies its
+    // SM sub-partition's FP64 pipe for the same time at any lane count, and
+    // one producer warp per sub-partition runs its chain at the same speed
+    // whatever its lane count; with the overlapped streams, full warps leave
+    // the most FP64 issue slots to the kernels running beside the producer.
+    // Without overlap a small batch is spread over about two warps per SM.
     if (ctx->orbit_spw > 0) {
       g.spw = ctx->orbit_spw;
+    } else if (ctx->overlap) {
+      g.spw = 32;
     } else {
       int target = std::max(1, 2 * ctx->sm_count);
       int want = (nsg + target - 1) / target, spw = 1;

@@ -12,9 +12,10 @@
 // The pair update uses the structure of jac_ij (ahl21.jl:734-750): rows of
 // body i are mj*K, -mj*K on (x,v)_i, (x,v)_j and rows of body j are -mi*K,
 // mi*K, so jac_ij * [J_i; J_j] = [mj u; -mi u] with u = K (J_i - J_j), plus
-// the two mass columns.  That is 54 FP64 operations per column instead of
-// 144 for the dense 12x12 block; the product is rounded differently from a
-// dense BLAS product, which the reference's BLAS leaves unspecified anyway.
+// the two mass columns (fused into the scaling FMA).  That is 54 FP64
+// operations per column instead of 144 for the dense 12x12 block; the
+// product is rounded differently from a dense BLAS product, which the
+// reference's BLAS leaves unspecified anyway.
 #pragma once
 #include "nbg_operators.cuh"
 
@@ -28,22 +29,24 @@ __device__ __forceinline__ void fold(double& s, double& e) {
 }
 
 // P[vr] = (A J)[velocity row vr] for the compact operator at record offset
-// roff: the FMA chain of the dense product in the reference's column order,
-// with the exact no-op terms (zero operator entries; mass rows of J, which
-// are unit rows) reduced to the single mass entry of this column.
+// roff: one FMA chain over the position rows of J, with the exact no-op
+// terms (zero operator entries; mass rows of J, which are unit rows) reduced
+// to the single mass entry of this column, which starts the chain.  Starting
+// from it costs no FP64 instruction, where adding it inside the chain would
+// cost a warp-wide issue slot for the few mass-column lanes; the summation
+// order of the reference's BLAS product is unspecified, so any order is as
+// faithful as another.
 template <int N, int BS>
 __device__ __forceinline__ void op_product(const double* J, const Rec& rec, int roff, int c, double* P) {
   const int cm = (c % 7 == 6) ? c / 7 : -1;  // body whose mass this column is
 #pragma unroll 1
   for (int vr = 0; vr < 3 * N; vr++) {
     const int rb = roff + vr * (4 * N);
-    double acc = 0.0;
+    double acc = (cm >= 0) ? rec.get(rb + 4 * cm + 3) : 0.0;
 #pragma unroll
-    for (int d = 0; d < N; d++) {
+    for (int d = 0; d < N; d++)
 #pragma unroll
       for (int p = 0; p < 3; p++) acc = fma(rec.get(rb + 4 * d + p), J[(6 * d + p) * BS], acc);
-      if (d == cm) acc = acc + rec.get(rb + 4 * d + 3);
-    }
     P[vr] = acc;
   }
 }
@@ -55,23 +58,18 @@ __device__ __forceinline__ void pair_apply(double* J, double* E, int c, int i, i
 #pragma unroll
   for (int l = 0; l < 6; l++) D[l] = J[(6 * i + l) * BS] - J[(6 * j + l) * BS];
   const double mi = rec.get(roff + PREC_MI), mj = rec.get(roff + PREC_MJ);
-  const bool ci = (c == 7 * i + 6), cj = (c == 7 * j + 6);
+  // the mass column of body i or j (at most one of them is this column)
+  // takes the pair's mass entries; every other column adds an exact zero
+  const int mc = (c == 7 * i + 6) ? PREC_MC6 : (c == 7 * j + 6) ? PREC_MC13 : -1;
 #pragma unroll
   for (int r = 0; r < 6; r++) {
     double u = rec.get(roff + r * 6) * D[0];
 #pragma unroll
     for (int l = 1; l < 6; l++) u = fma(rec.get(roff + r * 6 + l), D[l], u);
-    double ai = mj * u, aj = (-mi) * u;
-    if (ci) {
-      ai = ai + rec.get(roff + PREC_MC6 + r);
-      aj = aj + rec.get(roff + PREC_MC6 + 6 + r);
-    }
-    if (cj) {
-      ai = ai + rec.get(roff + PREC_MC13 + r);
-      aj = aj + rec.get(roff + PREC_MC13 + 6 + r);
-    }
-    kahan(J[(6 * i + r) * BS], E[(6 * i + r) * BS], ai);
-    kahan(J[(6 * j + r) * BS], E[(6 * j + r) * BS], aj);
+    const double ci = (mc >= 0) ? rec.get(roff + mc + r) : 0.0;
+    const double cj = (mc >= 0) ? rec.get(roff + mc + 6 + r) : 0.0;
+    kahan(J[(6 * i + r) * BS], E[(6 * i + r) * BS], fma(mj, u, ci));
+    kahan(J[(6 * j + r) * BS], E[(6 * j + r) * BS], fma(-mi, u, cj));
   }
 }
 

@@ -80,3 +80,53 @@ def test_deterministic_and_grad_free_times(c1_batch):
         P.check_transit_derivs(b1.view("dtdq0", q).reshape((3, ntt, 7, 3), order="F"), to.dtdq0, to.count)
         P.check_transit_derivs(b1.view("dtdelements", q).reshape((3, ntt, 7, 3), order="F"), to.dtdelements,
                                to.count, "dtdelements", to.dtdq0, so.jac_init)
+
+
+def test_c2_shape_batch():
+    """The 8-body workload's full batch (1024 systems, h = 0.06) over a
+    shortened span (tmax = 120 days, 2000 steps): determinism, bitwise
+    grad-free transit times, symplectic (x, v) block, clean status, and a
+    sample of systems against the oracle."""
+    els, h, _ = W.batch_8body(1024, seed=0)
+    tmax = 120.0
+    n, M = 8, 56
+    states = [nbg.State(W.ic_of(el)) for el in els]
+    ntt = nbg.TransitTiming(tmax, W.ic_of(els[0])).ntt + 2
+
+    def run(grad):
+        b = nbg.Batch([n] * len(els), 0, h, tmax, ntt, grad)
+        for q, s in enumerate(states):
+            b.set_system(q, s)
+        b.run()
+        return b
+
+    b1, b2, b0 = run(True), run(True), run(False)
+    for k in ("x", "v", "tt", "count", "jac_step", "dtdq0"):
+        assert np.array_equal(b1.arrays[k], b2.arrays[k]), k
+    assert np.array_equal(b1.arrays["tt"], b0.arrays["tt"])
+    bad = nbg._lib.NBG_STATUS_NONFINITE | nbg._lib.NBG_STATUS_NTT_OVERFLOW
+    assert np.all((b1.status & bad) == 0)
+    transits = int(b1.arrays["count"].sum())
+    assert transits > 1024 * 7 * 5
+    itmax = int(np.count_nonzero(b1.status & nbg._lib.NBG_STATUS_NEWTON_ITMAX))
+    assert itmax <= max(1, transits // 1000), (itmax, transits)
+    rows = [7 * b + r for b in range(n) for r in range(6)]
+    worst = 0.0
+    for q in range(0, len(els), 97):
+        J = b1.view("jac_step", q).reshape((M, M), order="F")
+        worst = max(worst, abs(np.linalg.det(J[np.ix_(rows, rows)]) - 1.0))
+    assert worst < 1e-8, worst
+    for q in (0, 1023):
+        s = states[q]
+        so = O.OState(s.x, s.v, s.m, jac_init=s.jac_init)
+        to = O.OTiming(n, ntt, 0)
+        O.integrate_transits(so, to, h, tmax)
+        P.check_counts(b1.view("count", q), to.count)
+        P.check_tt(b1.view("tt", q).reshape((n, ntt), order="F"), to.tt, to.count, tmax)
+        P.check_transit_derivs(b1.view("dtdq0", q).reshape((n, ntt, 7, n), order="F"), to.dtdq0, to.count)
+        gs = type("S", (), {})()
+        gs.x = b1.view("x", q).reshape((3, n), order="F")
+        gs.v = b1.view("v", q).reshape((3, n), order="F")
+        gs.jac_step = b1.view("jac_step", q).reshape((M, M), order="F")
+        gs.dqdt = b1.view("dqdt", q)
+        P.check_state(gs, so)
