@@ -288,7 +288,7 @@ def main():
     ctx = nbg.Context(local_rank)
     if args.chunk or args.serial:
         ctx.set_tuning(chunk_steps=args.chunk, overlap=0 if args.serial else -1)
-    chunk = args.chunk or 32  # the library's default chunk length
+    chunk = args.chunk or 64  # the library's default chunk length (not shortened at these sizes)
     if args.spw:
         ctx.set_orbit_lanes(args.spw)
     states, timings, hs, tms, nsteps = build_workload(nbg, args.workload, args.nsys, replica_seed(args.seed, rank))

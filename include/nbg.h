@@ -19,7 +19,8 @@
  *   - Return value: 0 on success, a negative NBG_E* code on failure; the
  *     message is available from nbg_last_error() on the calling thread.
  *   - The library never keeps a caller pointer after a call returns.
- *   - A context owns one CUDA stream and its device buffers; calls on one
+ *   - A context owns its CUDA streams (one, plus two more while the
+ *     overlapped chunk pipeline is on) and its device buffers; calls on one
  *     context must not overlap.  Different contexts may be used from
  *     different threads.
  */
@@ -165,8 +166,9 @@ int nbg_batch_integrate_transits_noalloc(nbg_context* ctx, int nsys, const nbg_s
                                          int64_t* count, uint32_t* status);
 
 /* Tuning knobs of a context.  Results do not depend on them.
- * chunk_steps: integration steps per producer/consumer chunk (default 32;
- *   0 keeps the current value);
+ * chunk_steps: integration steps per producer/consumer chunk (default 64,
+ *   shortened for batches whose per-chunk operator records would pass
+ *   4 GiB; 0 keeps the current value);
  * overlap: 1 (default) runs the orbit producer on its own stream one chunk
  *   ahead of the transit searches, operator kernels and Jacobian consumer
  *   (two more streams of the context); 0 runs everything on one stream;

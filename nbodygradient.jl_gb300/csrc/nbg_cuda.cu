@@ -177,7 +177,7 @@ struct nbg_context {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::map<std::string, Buf> pool;
-  int chunk_steps = 32;
+  int chunk_steps = 64;
   int overlap = 1;  // orbit producer on its own stream, one chunk ahead of the rest
   int orbit_spw = 0;  // 0: automatic
   int sm_count = 0;
@@ -330,7 +330,20 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     NBG_CUDA(cudaMemcpyAsync(d_offdq, b.data(), sizeof(long long) * nsys, cudaMemcpyHostToDevice, st));
     NBG_CUDA(cudaStreamSynchronize(st));  // host vectors a, b go out of scope
   }
-  const int K = std::max(1, ctx->chunk_steps);
+  // Steps per chunk: the context's setting, shortened (not below 8) where a
+  // group's operator records for one chunk would pass 4 GiB per buffer half.
+  int K = std::max(1, ctx->chunk_steps);
+  for (auto& kv : groups) {
+    const GroupPlan& gp = kv.second;
+    if (!gp.grad) continue;
+    int npk = 0;
+    for (int i = 0; i < gp.N - 1; i++)
+      for (int j = i + 1; j < gp.N; j++)
+        if (!((gp.kick >> pair_bit(i, j, gp.N)) & 1)) npk++;
+    const double per_step = 8.0 * step_record_size(gp.N, npk, gp.kick != 0) * (((gp.systems.size() + 31) / 32) * 32);
+    const int kmax = (int)std::min(4096.0, std::floor(4294967296.0 / per_step));
+    K = std::min(K, std::max(std::min(K, 8), kmax));
+  }
   // ---- per-group device state
   std::vector<GroupArgs> gargs;
   std::vector<GroupArgs> ghalf;  // the same groups on the second half of the per-chunk buffers
