@@ -248,6 +248,90 @@ def run_reference(args, nbg, rank):
     print(json.dumps(line), flush=True)
 
 
+def serve_stream(nbg, srv, pool, rate, nreq, seed, timeout_s):
+    """Poisson arrivals (rate requests/s) of nreq requests drawn from pool;
+    returns (infos, wall seconds from first arrival to last completion)."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, nreq) if rate > 0 else np.zeros(nreq)
+    picks = rng.integers(0, len(pool), nreq)
+    ids, infos, lock = {}, [], threading.Lock()
+    done = threading.Event()
+    t_start = time.perf_counter()
+
+    def client():
+        t = t_start
+        for q in range(nreq):
+            t += gaps[q]
+            d = t - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            s0, ic, h, tmax, grad = pool[picks[q]]
+            s = s0.copy()
+            tt = nbg.TransitTiming(tmax, ic)
+            rid = srv.submit(s, tt, nbg.Integrator(nbg.ahl21, h, 0.0, tmax), grad)
+            with lock:
+                ids[rid] = (s, tt)
+
+    def collector():
+        got = 0
+        while got < nreq:
+            try:
+                rid = srv.wait_any(timeout_ms=int(timeout_s * 1000))
+            except nbg.NbgError:
+                break
+            while True:
+                with lock:
+                    st = ids.pop(rid, None)
+                if st is not None:
+                    break
+                time.sleep(1e-4)  # the client has not recorded this id yet
+            infos.append(srv.result(rid, st[0], st[1]))
+            got += 1
+        done.set()
+
+    tc, tr = threading.Thread(target=client), threading.Thread(target=collector)
+    tc.start()
+    tr.start()
+    tc.join()
+    tr.join()
+    return infos, time.perf_counter() - t_start
+
+
+def run_serve(args, nbg):
+    """Serving (C4): Poisson streams of single systems drawn as batch_uneven,
+    50 % grad=true; system-steps/s and p50/p99 latency per body count."""
+    W = nbg.workloads
+    els, hs, tms = W.batch_uneven(args.serve_pool, args.seed + 11)
+    rng = np.random.default_rng(args.seed + 12)
+    pool = []
+    for el, h, tmax in zip(els, hs, tms):
+        ic = W.ic_of(el)
+        tmax = min(tmax, args.serve_tmax_max) if args.serve_tmax_max > 0 else tmax
+        pool.append((nbg.State(ic), ic, h, tmax, bool(rng.integers(0, 2))))
+    rates = [float(r) for r in args.serve_rates.split(",")]
+    out = []
+    for k, rate in enumerate(rates):
+        with nbg.Server(slots_per_group=args.serve_slots, chunk_steps=args.serve_chunk) as srv:
+            infos, wall = serve_stream(nbg, srv, pool, rate, args.serve_requests, args.seed + 100 + k,
+                                       args.serve_timeout)
+            st = srv.stats()
+        ok = [i for i in infos if i["rc"] == 0]
+        steps = sum(i["nsteps"] for i in ok)
+        per_n = {}
+        for nb in sorted({i["n"] for i in ok}):
+            lat = np.array([i["latency_ms"] for i in ok if i["n"] == nb])
+            per_n[str(nb)] = {"requests": int(len(lat)), "p50_ms": float(np.percentile(lat, 50)),
+                              "p99_ms": float(np.percentile(lat, 99))}
+        lat = np.array([i["latency_ms"] for i in ok]) if ok else np.zeros(1)
+        out.append({"rate_per_s": rate, "requests": args.serve_requests, "completed": len(ok),
+                    "system_steps_per_s": steps / wall, "wall_s": wall,
+                    "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                    "queue_p99_ms": float(np.percentile([i["queue_ms"] for i in ok], 99)) if ok else None,
+                    "per_n": per_n, "chunks": st["chunks"], "kernels": st["kernels"], "groups": st["groups"]})
+        print(json.dumps({"serve": out[-1]}), flush=True)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -266,6 +350,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--serve", action="store_true", help="serving (C4): Poisson request streams, then exit")
+    ap.add_argument("--serve-rates", default="4,16,64,0", help="request rates per second (0 = all at once)")
+    ap.add_argument("--serve-requests", type=int, default=256)
+    ap.add_argument("--serve-pool", type=int, default=512)
+    ap.add_argument("--serve-slots", type=int, default=256)
+    ap.add_argument("--serve-chunk", type=int, default=32)
+    ap.add_argument("--serve-tmax-max", type=float, default=0.0, help="cap on a request's tmax (0: none)")
+    ap.add_argument("--serve-timeout", type=float, default=600.0)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -285,6 +377,9 @@ def main():
 
     import torch
     torch.cuda.set_device(local_rank)
+    if args.serve:
+        run_serve(args, nbg)
+        return
     ctx = nbg.Context(local_rank)
     if args.chunk or args.serial:
         ctx.set_tuning(chunk_steps=args.chunk, overlap=0 if args.serial else -1)

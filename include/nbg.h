@@ -165,6 +165,86 @@ int nbg_batch_integrate_transits_noalloc(nbg_context* ctx, int nsys, const nbg_s
                                          const double* jac_init, double* tt, double* dtdq0, double* dtdelements,
                                          int64_t* count, uint32_t* status);
 
+/*
+ * Request server: continuous batching of single-system requests.
+ *
+ * Replaces: the same (intr::Integrator)(s::State{Float64}, tt::TransitTiming;
+ * grad) call as nbg_integrate_transits (src/transits/Transits.jl:140-180),
+ * issued as independent requests from any number of host threads.  A request
+ * is a State plus a fresh TransitTiming (count = 0, tt / dtdq0 / dtdelements
+ * zero).  Requests with the same body count, grad flag and pair pattern share
+ * a group of device-resident slots; each group advances all its slots by
+ * chunk_steps steps per chunk on its own CUDA stream, and a request that
+ * arrives while others run takes a free slot at the next chunk boundary of
+ * its group (its first step runs in that chunk).  A slot holds its system's
+ * state and jac_step on the device from admission to its last step.
+ * Admission is by HBM footprint: half of hbm_budget_bytes is an output arena
+ * from which each admitted request takes its tt / dtdq0 / dtdelements block
+ * (a request waits while the arena is full); the other half holds the groups'
+ * slot buffers (a request whose new group does not fit fails NBG_ENOMEM).
+ * Results are bitwise the same whether a request runs alone or among others.
+ * Requests not yet admitted when the server stops are cancelled
+ * (NBG_ECANCELLED); admitted ones run to completion.
+ */
+typedef struct nbg_server nbg_server;
+
+typedef struct {
+  int32_t slots_per_group;   /* slots per (n, grad, pair pattern) group; 0 = 256 (rounded up to 32) */
+  int32_t chunk_steps;       /* steps per chunk; 0 = 32                                   */
+  int32_t max_inflight;      /* chunks a group may have queued on the GPU; 0 = 2          */
+  int32_t orbit_lanes;       /* orbit producer systems per warp (1..32); 0 = 32           */
+  uint64_t hbm_budget_bytes; /* device memory the server may hold; 0 = a quarter of free  */
+} nbg_server_config;
+
+typedef struct {
+  int64_t id;
+  int32_t n, grad;
+  int64_t nsteps;
+  double queue_ms;   /* enqueue -> admitted into a slot                    */
+  double run_ms;     /* admitted -> results in the server's host buffer    */
+  double latency_ms; /* enqueue -> results in the server's host buffer     */
+  uint32_t status;   /* NBG_STATUS_* bits                                  */
+  int32_t rc;        /* NBG_OK or the request's error code                 */
+} nbg_request_info;
+
+typedef struct {
+  int64_t submitted, admitted, completed, failed, running, pending;
+  int64_t chunks, kernels;   /* chunk launches and kernel launches so far */
+  uint64_t hbm_groups;       /* bytes held by the groups' slot buffers     */
+  uint64_t hbm_outputs_in_use; /* bytes of the output arena in use         */
+  uint64_t hbm_budget;
+  int32_t groups, pad;
+} nbg_server_stats_t;
+
+/* Start a server (and its host thread) on CUDA device `device`; cfg may be NULL. */
+int nbg_server_start(int device, const nbg_server_config* cfg, nbg_server** out);
+
+/* Queue one request; the arrays are copied before the call returns.  desc
+ * as for the batched calls; t0 is s.t.  jac_step, jac_error, jac_init and
+ * dqdt may be NULL when desc->grad == 0.  *id receives the request id. */
+int nbg_server_enqueue(nbg_server* srv, const nbg_system_desc* desc, double t0, const double* x, const double* v,
+                       const double* m, const double* xerror, const double* verror, const double* jac_step,
+                       const double* jac_error, const double* dqdt, const uint8_t* pair, const double* jac_init,
+                       int64_t* id);
+
+/* Wait up to timeout_ms (< 0: no limit) for the next completed request not
+ * yet collected; NBG_ETIMEOUT if none completes in time. */
+int nbg_server_wait_any(nbg_server* srv, int32_t timeout_ms, int64_t* id);
+
+/* Wait up to timeout_ms (< 0: no limit) for request `id`, copy its results
+ * into the (non-NULL) output arrays -- the State fields as updated by the
+ * integration, s.t, and the TransitTiming tt, dtdq0, dtdelements and count
+ * -- and release it.  info (may be NULL) receives its latency and status.
+ * Returns the request's own error code if it failed. */
+int nbg_server_poll(nbg_server* srv, int64_t id, int32_t timeout_ms, double* t, double* x, double* v,
+                    double* xerror, double* verror, double* jac_step, double* jac_error, double* dqdt, double* tt,
+                    double* dtdq0, double* dtdelements, int64_t* count, nbg_request_info* info);
+
+int nbg_server_stats(nbg_server* srv, nbg_server_stats_t* out);
+
+/* Cancel requests not yet admitted, finish the running ones, free the server. */
+int nbg_server_stop(nbg_server* srv);
+
 /* Tuning knobs of a context.  Results do not depend on them.
  * chunk_steps: integration steps per producer/consumer chunk (default 64,
  *   shortened for batches whose per-chunk operator records would pass

@@ -25,7 +25,7 @@ from ._lib import Context, NbgError, SystemDesc, default_context, device_info
 from .ics import CartesianIC, Elements, ElementsIC, hierarchy_nested, init_nbody, kepler_init
 
 __all__ = ["Elements", "ElementsIC", "CartesianIC", "State", "TransitTiming", "Integrator", "ahl21", "set_state",
-           "Context", "NbgError", "default_context", "device_info", "integrate_transits_batch", "Batch",
+           "Context", "NbgError", "default_context", "device_info", "integrate_transits_batch", "Batch", "Server",
            "hierarchy_nested", "init_nbody", "kepler_init"]
 
 
@@ -268,6 +268,80 @@ class Batch:
             vp("verror"), vp("jac_step"), vp("jac_error"), vp("dqdt"), vp("pair"), vp("jac_init"), vp("tt"),
             vp("dtdq0"), vp("dtdelements"), vp("count"), ctypes.c_void_p(self.status.ctypes.data)))
         return self
+
+
+class Server:
+    """Continuous-batching request server (nbg_server_* in include/nbg.h).
+
+    submit(s, tt, intr, grad) queues intr(s, tt; grad) for a State and a
+    fresh TransitTiming and returns a request id; result(id, s, tt) waits for
+    it, fills s and tt in place exactly as intr(s, tt; grad) would, and returns
+    the request's latency record.  Requests from any thread; requests that
+    arrive while others run join them on the GPU at the next chunk boundary.
+    """
+
+    def __init__(self, device=0, slots_per_group=0, chunk_steps=0, max_inflight=0, orbit_lanes=0,
+                 hbm_budget_bytes=0):
+        import ctypes
+        L = _lib.load()
+        cfg = _lib.ServerConfig(int(slots_per_group), int(chunk_steps), int(max_inflight), int(orbit_lanes),
+                                int(hbm_budget_bytes))
+        h = ctypes.c_void_p()
+        _lib.check(L.nbg_server_start(int(device), ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+
+    def submit(self, s, tt, intr, grad=True):
+        import ctypes
+        if tt.count.any():
+            raise ValueError("the server takes a fresh TransitTiming (count == 0)")
+        L = _lib.load()
+        p = _lib.ptr
+        d = SystemDesc(s.n, tt.ti - 1, int(bool(grad)), tt.ntt, float(intr.h), float(intr.tmax))
+        rid = ctypes.c_int64()
+        _lib.check(L.nbg_server_enqueue(self._h, ctypes.byref(d), float(s.t[0]), p(s.x), p(s.v), p(s.m),
+                                        p(s.xerror), p(s.verror), p(s.jac_step), p(s.jac_error), p(s.dqdt),
+                                        p(s.pair, _lib._U8), p(s.jac_init), ctypes.byref(rid)))
+        return rid.value
+
+    def wait_any(self, timeout_ms=-1):
+        import ctypes
+        rid = ctypes.c_int64()
+        _lib.check(_lib.load().nbg_server_wait_any(self._h, int(timeout_ms), ctypes.byref(rid)))
+        return rid.value
+
+    def result(self, rid, s, tt, timeout_ms=-1):
+        """Collect request rid into (s, tt); returns its info as a dict."""
+        import ctypes
+        info = _lib.RequestInfo()
+        p = _lib.ptr
+        _lib.check(_lib.load().nbg_server_poll(
+            self._h, int(rid), int(timeout_ms), p(s.t), p(s.x), p(s.v), p(s.xerror), p(s.verror), p(s.jac_step),
+            p(s.jac_error), p(s.dqdt), p(tt.tt), p(tt.dtdq0), p(tt.dtdelements), p(tt.count, _lib._I64),
+            ctypes.byref(info)))
+        return {k: getattr(info, k) for k, _ in _lib.RequestInfo._fields_}
+
+    def stats(self):
+        import ctypes
+        st = _lib.ServerStats()
+        _lib.check(_lib.load().nbg_server_stats(self._h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in _lib.ServerStats._fields_}
+
+    def stop(self):
+        if self._h is not None and self._h.value:
+            h, self._h = self._h, None
+            _lib.check(_lib.load().nbg_server_stop(h))
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.stop()
+
+    def __del__(self):
+        try:
+            self.stop()
+        except Exception:
+            pass
 
 
 def integrate_transits_batch(states, timings, h, tmax, grad=True, ctx=None):

@@ -33,6 +33,8 @@ EXPORTS = (
     "nbg_set_tuning", "nbg_last_timing", "nbg_last_launch_count", "nbg_fp64_peak",
     "nbg_set_profiling", "nbg_last_kernel_stats", "nbg_set_orbit_lanes",
     "nbg_batch_integrate_transits_noalloc",
+    "nbg_server_start", "nbg_server_enqueue", "nbg_server_wait_any", "nbg_server_poll", "nbg_server_stats",
+    "nbg_server_stop",
 )
 
 
@@ -51,6 +53,26 @@ class DeviceInfo(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char * 128), ("sm_count", ctypes.c_int), ("cc_major", ctypes.c_int),
                 ("cc_minor", ctypes.c_int), ("total_mem", ctypes.c_size_t), ("min_bodies", ctypes.c_int),
                 ("max_bodies", ctypes.c_int)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("slots_per_group", ctypes.c_int32), ("chunk_steps", ctypes.c_int32),
+                ("max_inflight", ctypes.c_int32), ("orbit_lanes", ctypes.c_int32),
+                ("hbm_budget_bytes", ctypes.c_uint64)]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_int64), ("n", ctypes.c_int32), ("grad", ctypes.c_int32), ("nsteps", ctypes.c_int64),
+                ("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+                ("status", ctypes.c_uint32), ("rc", ctypes.c_int32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("admitted", ctypes.c_int64), ("completed", ctypes.c_int64),
+                ("failed", ctypes.c_int64), ("running", ctypes.c_int64), ("pending", ctypes.c_int64),
+                ("chunks", ctypes.c_int64), ("kernels", ctypes.c_int64), ("hbm_groups", ctypes.c_uint64),
+                ("hbm_outputs_in_use", ctypes.c_uint64), ("hbm_budget", ctypes.c_uint64),
+                ("groups", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
 _D = ctypes.POINTER(ctypes.c_double)
@@ -98,6 +120,14 @@ def load(build_if_missing=True):
     L.nbg_set_profiling.argtypes = [_VP, ctypes.c_int]
     L.nbg_set_orbit_lanes.argtypes = [_VP, ctypes.c_int]
     L.nbg_last_kernel_stats.argtypes = [_VP, _I64, _I64]
+    L.nbg_server_start.argtypes = [ctypes.c_int, ctypes.POINTER(ServerConfig), ctypes.POINTER(_VP)]
+    L.nbg_server_enqueue.argtypes = [_VP, ctypes.POINTER(SystemDesc), ctypes.c_double, _D, _D, _D, _D, _D, _D, _D,
+                                     _D, _U8, _D, _I64]
+    L.nbg_server_wait_any.argtypes = [_VP, ctypes.c_int32, _I64]
+    L.nbg_server_poll.argtypes = [_VP, ctypes.c_int64, ctypes.c_int32, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D,
+                                  _I64, ctypes.POINTER(RequestInfo)]
+    L.nbg_server_stats.argtypes = [_VP, ctypes.POINTER(ServerStats)]
+    L.nbg_server_stop.argtypes = [_VP]
     _lib = L
     return L
 

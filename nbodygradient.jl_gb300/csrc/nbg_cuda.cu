@@ -19,17 +19,11 @@
 #include <vector>
 
 #include "../../include/nbg.h"
-#include "nbg_layout.cuh"
+#include "nbg_internal.cuh"
 
 using namespace nbg;
 
 // ===================================================================== kernels
-
-// Per-system offsets into the caller's packed arrays.
-struct SysOff {
-  long long x, m, J, dqdt, pair, tt, dq, cnt;
-  int n, ntt, grad, pad;
-};
 
 // Gather the caller-layout arrays of one group's systems into its SoA state.
 __global__ void pack_state_kernel(int N, int S, const int* sysidx, const SysOff* off, const double* x,
@@ -118,11 +112,14 @@ __global__ void unpack_jac_kernel(int N, int S, const int* sysidx, const SysOff*
 }
 
 // calc_dtdelements! (timing.jl:112-123): one thread per output entry of one
-// system; transits beyond min(count, ntt) are left untouched.
-__global__ void dtdelements_kernel(int nsys, const SysOff* off, const double* dtdq0, const double* jac_init,
-                                   double* dtdel, const long long* count) {
-  const int gs = blockIdx.y + gridDim.y * blockIdx.z;
-  if (gs >= nsys) return;
+// system; transits beyond min(count, ntt) are left untouched.  Systems are
+// list[y] (or y itself without a list); with after_dtdq0 a system's output
+// block follows its dtdq0 block in the dtdq0 array.
+__global__ void dtdelements_kernel(int nsys, const int* list, const SysOff* off, const double* dtdq0,
+                                   const double* jac_init, double* dtdel, const long long* count, int after_dtdq0) {
+  const int y = blockIdx.y + gridDim.y * blockIdx.z;
+  if (y >= nsys) return;
+  const int gs = list ? list[y] : y;
   const SysOff o = off[gs];
   if (!o.grad) return;
   const int n = o.n, ntt = o.ntt, M = 7 * n;
@@ -139,7 +136,7 @@ __global__ void dtdelements_kernel(int nsys, const SysOff* off, const double* dt
       for (int q = 0; q < 7; q++)
         acc = acc + dtdq0[o.dq + j + (long long)n * (c + (long long)ntt * (q + 7LL * p))] *
                         jac_init[o.J + (7 * p + q) + (long long)M * (7 * k + l)];
-    dtdel[o.dq + e] = acc;
+    dtdel[o.dq + (after_dtdq0 ? tot : 0) + e] = acc;
   }
 }
 
@@ -147,8 +144,10 @@ __global__ void dtdelements_kernel(int nsys, const SysOff* off, const double* dt
 
 
 namespace {
-
 thread_local std::string g_last_error;
+}  // namespace
+
+namespace nbg {
 
 int set_error(int code, const char* fmt, ...) {
   char buf[512];
@@ -160,11 +159,56 @@ int set_error(int code, const char* fmt, ...) {
   return code;
 }
 
-#define NBG_CUDA(call)                                                                          \
-  do {                                                                                          \
-    cudaError_t e_ = (call);                                                                    \
-    if (e_ != cudaSuccess) return set_error(NBG_ECUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
-  } while (0)
+long long steps_of(double h, double tmax) {
+  double q = std::nearbyint(tmax / h);  // round(Int64, tmax/h): ties to even
+  long long n = (long long)q;
+  return n < 0 ? -n : n;
+}
+
+// check_step (src/integrator/Integrator.jl:249-259)
+double check_step(double t0, double tmax) {
+  auto sgn = [](double x) { return x > 0 ? 1.0 : (x < 0 ? -1.0 : x); };
+  if (std::fabs(tmax) > std::fabs(t0)) return sgn(tmax);
+  if (sgn(tmax) != sgn(t0)) return sgn(tmax);
+  return -1.0 * sgn(tmax);
+}
+
+void launch_pack_state(int N, int S, const int* sysidx, const SysOff* off, const double* x, const double* v,
+                       const double* xe, const double* ve, const double* m, const double* dqdt,
+                       const long long* count, const GroupArgs& g, cudaStream_t st) {
+  pack_state_kernel<<<(S + 127) / 128, 128, 0, st>>>(N, S, sysidx, off, x, v, xe, ve, m, dqdt, count, g.x, g.v,
+                                                      g.xe, g.ve, g.m, g.dqdt, g.count);
+}
+
+void launch_unpack_state(int N, int S, int grad, const int* sysidx, const SysOff* off, double* x, double* v,
+                         double* xe, double* ve, double* dqdt, long long* count, const GroupArgs& g,
+                         cudaStream_t st) {
+  unpack_state_kernel<<<(S + 127) / 128, 128, 0, st>>>(N, S, grad, sysidx, off, x, v, xe, ve, dqdt, count, g.x,
+                                                        g.v, g.xe, g.ve, g.dqdt, g.count);
+}
+
+void launch_pack_jac(int N, int S, const int* sysidx, const SysOff* off, const double* J, const double* E,
+                     const GroupArgs& g, int* bad, cudaStream_t st) {
+  const long long tot = (long long)S * 49 * N * N;
+  pack_jac_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(N, S, sysidx, off, J, E, g.Jint, g.Eint, bad);
+}
+
+void launch_unpack_jac(int N, int S, const int* sysidx, const SysOff* off, double* J, double* E,
+                       const GroupArgs& g, cudaStream_t st) {
+  const long long tot = (long long)S * 42 * N * N;
+  unpack_jac_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(N, S, sysidx, off, J, E, g.Jint, g.Eint);
+}
+
+void launch_dtdelements(int nlist, const int* list, const SysOff* off, const double* dtdq0, const double* jac_init,
+                        double* dtdel, const long long* count, bool after_dtdq0, cudaStream_t st) {
+  if (nlist <= 0) return;
+  dim3 grid(8, std::min(nlist, 65535), (nlist + 65534) / 65535);
+  dtdelements_kernel<<<grid, 256, 0, st>>>(nlist, list, off, dtdq0, jac_init, dtdel, count, after_dtdq0 ? 1 : 0);
+}
+
+}  // namespace nbg
+
+namespace {
 
 struct Buf {
   void* p = nullptr;
@@ -254,18 +298,17 @@ const SeedFn kSeed[NBG_MAX_BODIES + 1] = {nullptr, nullptr, launch_seed<2>, laun
                                           launch_seed<5>, launch_seed<6>, launch_seed<7>, launch_seed<8>,
                                           launch_seed<9>, launch_seed<10>};
 
-long long steps_of(double h, double tmax) {
-  double q = std::nearbyint(tmax / h);  // round(Int64, tmax/h): ties to even
-  long long n = (long long)q;
-  return n < 0 ? -n : n;
-}
-// check_step (src/integrator/Integrator.jl:249-259)
-double check_step(double t0, double tmax) {
-  auto sgn = [](double x) { return x > 0 ? 1.0 : (x < 0 ? -1.0 : x); };
-  if (std::fabs(tmax) > std::fabs(t0)) return sgn(tmax);
-  if (sgn(tmax) != sgn(t0)) return sgn(tmax);
-  return -1.0 * sgn(tmax);
-}
+}  // namespace
+
+namespace nbg {
+int launch_group_orbit(int N, const GroupArgs& g, int chunk, cudaStream_t st) { return kOrbit[N](g, chunk, st); }
+int launch_group_transit(int N, const GroupArgs& g, int chunk, cudaStream_t st) { return kTransit[N](g, chunk, st); }
+int launch_group_operators(int N, const GroupArgs& g, int chunk, cudaStream_t st) { return kOps[N](g, chunk, st); }
+int launch_group_jacobian(int N, const GroupArgs& g, int chunk, cudaStream_t st) { return kJac[N](g, chunk, st); }
+int launch_group_seed(int N, const GroupArgs& g, cudaStream_t st) { return kSeed[N](g, st); }
+}  // namespace nbg
+
+namespace {
 
 struct GroupPlan {
   int N, grad;
@@ -581,7 +624,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
   }
   {
     dim3 grid(8, std::min(nsys, 65535), (nsys + 65534) / 65535);
-    dtdelements_kernel<<<grid, 256, 0, st>>>(nsys, d_off, d_dq0, d_jinit, d_dtdel, d_count);
+    dtdelements_kernel<<<grid, 256, 0, st>>>(nsys, nullptr, d_off, d_dq0, d_jinit, d_dtdel, d_count, 0);
     ctx->last_launches++;
   }
   // s.t = t0 + nsteps * h (Transits.jl:161 at the last step)
@@ -896,7 +939,7 @@ int run_batch_noalloc(nbg_context* ctx, NoallocPlan& P, int nsys, const nbg_syst
   }
   {
     dim3 grid(8, nsys, 1);
-    dtdelements_kernel<<<grid, 256, 0, st>>>(nsys, d_off, d_dq0, d_jinit, d_dtdel, d_count);
+    dtdelements_kernel<<<grid, 256, 0, st>>>(nsys, nullptr, d_off, d_dq0, d_jinit, d_dtdel, d_count, 0);
     ctx->last_launches++;
   }
   // s.t = t0 + nsteps * h (Transits.jl:161 at the last step)

@@ -25,7 +25,7 @@ __global__ void __launch_bounds__(PROD_BS) orbit_chunk_kernel(GroupArgs g, int c
   if (s >= g.S || g.sysidx[s] < 0) return;
   const int S = g.S;
   const long long nst = g.nsteps[s];
-  const long long k0 = (long long)chunk * g.K;
+  const long long k0 = chunk_first_step(g, chunk, s);
   if (k0 >= nst) return;
   Sys<N> st;
   Work<N> w;
@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(OPS_BS) operator_pair_kernel(GroupArgs g, int 
   const long long rest = L / S;
   const int slot = (int)(rest % np2), kk = (int)(rest / np2);
   if (g.sysidx[s] < 0) return;
-  if ((long long)chunk * g.K + kk >= g.nsteps[s]) return;
+  if (chunk_first_step(g, chunk, s) + kk >= g.nsteps[s]) return;
   const uint64_t kick = g.kick;
   Rec cap{g.pcap + (size_t)kk * np2 * PCAP * S + s, S};
   Rec rec{g.steprec + (size_t)kk * g.R * S + s, S};
@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(OPS_BS) operator_phi_kernel(GroupArgs g, int c
   if (L >= (long long)g.K * S) return;
   const int s = (int)(L % S), kk = (int)(L / S);
   if (g.sysidx[s] < 0) return;
-  if ((long long)chunk * g.K + kk >= g.nsteps[s]) return;
+  if (chunk_first_step(g, chunk, s) + kk >= g.nsteps[s]) return;
   const uint64_t kick = g.kick;
   const double h = g.h[s];
   Rec xs{g.xsnap + (size_t)kk * snap_count(kick != 0) * 3 * N * S + s, S};
@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(CONS_BS) jacobian_chunk_kernel(GroupArgs g, in
   if (s >= g.S || g.sysidx[s] < 0) return;
   const int S = g.S;
   const long long nst = g.nsteps[s];
-  const long long k0 = (long long)chunk * g.K;
+  const long long k0 = chunk_first_step(g, chunk, s);
   if (k0 >= nst) return;
   double* J = smem + threadIdx.x;
   double* E = smem + R6 * CONS_BS + threadIdx.x;

@@ -43,6 +43,9 @@ struct GroupArgs {
   long long* count;  // [N][S]
   double *t0, *h, *hI;
   long long* nsteps;
+  // first chunk of each slot, in steps (null: every system starts at chunk 0);
+  // the request server admits systems into running groups this way
+  const long long* kbase;
   int *ntt, *ti, *sysidx;
   unsigned int* status;
   // packed outputs in the caller's layout, indexed by global system
@@ -67,6 +70,11 @@ struct GroupArgs {
   double* pcap;   // [K][2 npk][28][S]: Kepler-pair parameters
   double* xsnap;  // [K][snaps][3N][S]: positions at the correctors (and kicks)
 };
+
+// Index of the first step of chunk `chunk` for the system in slot s.
+__device__ __forceinline__ long long chunk_first_step(const GroupArgs& g, int chunk, int s) {
+  return (long long)chunk * g.K - (g.kbase ? g.kbase[s] : 0);
+}
 
 template <int N> int launch_orbit(const GroupArgs& g, int chunk, cudaStream_t st);
 template <int N> int launch_jac(const GroupArgs& g, int chunk, cudaStream_t st);

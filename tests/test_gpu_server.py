@@ -1,0 +1,155 @@
+"""The request server (nbg_server_* through its C ABI) on the GPU.
+
+Requests of mixed body count, grad flag, pair pattern and length arrive
+while others run; each result must be bitwise the same as the same request
+served alone, bitwise the same as the batched entry point's, and within the
+parity tolerances of the oracle.
+"""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+import nbg
+import oracle_lib as O
+import parity as P
+from conftest import has_gpu
+from nbg import workloads as W
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not has_gpu(), reason="needs a CUDA GPU")]
+
+FIELDS_S = ("t", "x", "v", "xerror", "verror", "jac_step", "jac_error", "dqdt")
+FIELDS_T = ("tt", "dtdq0", "dtdelements", "count")
+
+
+def make_requests(nreq=24, seed=11):
+    """(State, TransitTiming, Integrator, grad) tuples: N in 2..6, 20..160 steps."""
+    rng = np.random.default_rng(seed)
+    els, hs, _ = W.batch_uneven(nreq, seed=seed, nmin=2, nmax=6)
+    reqs = []
+    for q, (el, h) in enumerate(zip(els, hs)):
+        tmax = float(h * rng.integers(20, 161))
+        ic = W.ic_of(el)
+        s = nbg.State(ic)
+        if q % 7 == 3 and s.n >= 3:
+            s.pair[0, 1] = s.pair[1, 0] = 1  # a kick pair: its own group
+        tt = nbg.TransitTiming(tmax, ic)
+        reqs.append((s, tt, nbg.Integrator(nbg.ahl21, h, 0.0, tmax), bool(q % 2 == 0)))
+    return reqs
+
+
+def fresh(req):
+    """A copy of the request's State and a zeroed TransitTiming of the same shape."""
+    s, tt, intr, grad = req
+    t2 = nbg.TransitTiming.__new__(nbg.TransitTiming)
+    t2.__dict__.update(n=tt.n, ntt=tt.ntt, ti=tt.ti, occs=list(tt.occs))
+    for k in ("tt", "dtdq0", "dtdelements", "count"):
+        setattr(t2, k, np.zeros_like(getattr(tt, k), order="F"))
+    return s.copy(), t2, intr, grad
+
+
+def assert_same(a, b):
+    (sa, ta), (sb, tb) = a, b
+    for k in FIELDS_S:
+        assert np.array_equal(getattr(sa, k), getattr(sb, k)), k
+    for k in FIELDS_T:
+        assert np.array_equal(getattr(ta, k), getattr(tb, k)), k
+
+
+def serve_mix(srv, reqs, jitter_ms=3.0, seed=0):
+    """Submit every request from a client thread at random intervals; collect all."""
+    rng = np.random.default_rng(seed)
+    outs = [fresh(r) for r in reqs]
+    ids = [None] * len(reqs)
+
+    def client():
+        for q, (s, tt, intr, grad) in enumerate(outs):
+            ids[q] = srv.submit(s, tt, intr, grad)
+            time.sleep(rng.uniform(0, jitter_ms) * 1e-3)
+
+    th = threading.Thread(target=client)
+    th.start()
+    th.join()
+    infos = []
+    for q, (s, tt, intr, grad) in enumerate(outs):
+        infos.append(srv.result(ids[q], s, tt, timeout_ms=120000))
+    return [(s, tt) for s, tt, _, _ in outs], infos
+
+
+def test_mix_is_bitwise_alone_and_batched():
+    reqs = make_requests()
+    with nbg.Server(slots_per_group=32, chunk_steps=16) as srv:
+        mix, infos = serve_mix(srv, reqs)
+        assert all(i["rc"] == 0 for i in infos)
+        st = srv.stats()
+        assert st["completed"] == len(reqs) and st["running"] == 0 and st["pending"] == 0
+        assert st["groups"] >= 4
+        # each request alone on the same server
+        for q, r in enumerate(reqs):
+            s, tt, intr, grad = fresh(r)
+            srv.result(srv.submit(s, tt, intr, grad), s, tt, timeout_ms=120000)
+            assert_same(mix[q], (s, tt))
+    # the batched entry point gives the same bits
+    for q, r in enumerate(reqs):
+        s, tt, intr, grad = fresh(r)
+        b = nbg.Batch([s.n], [tt.ti - 1], intr.h, intr.tmax, [tt.ntt], grad)
+        b.set_system(0, s, tt)
+        b.run()
+        b.get_system(0, s, tt)
+        assert_same(mix[q], (s, tt))
+
+
+def test_served_results_match_oracle():
+    reqs = make_requests(8, seed=5)
+    with nbg.Server(slots_per_group=32, chunk_steps=8) as srv:
+        mix, _ = serve_mix(srv, reqs, seed=1)
+    for (s, tt), (s0, tt0, intr, grad) in zip(mix, reqs):
+        so = O.OState(s0.x, s0.v, s0.m, jac_init=s0.jac_init, t=0.0, pair=s0.pair)
+        to = O.OTiming(s0.n, tt0.ntt, 0)
+        O.integrate_transits(so, to, intr.h, intr.tmax, grad=grad)
+        P.check_counts(tt.count, to.count)
+        P.check_tt(tt.tt, to.tt, to.count, intr.tmax)
+        assert s.t[0] == so.t[0]
+        P.check_state(s, so, check_jac=grad)
+        if grad:
+            P.check_transit_derivs(tt.dtdq0, to.dtdq0, to.count, "dtdq0")
+            P.check_transit_derivs(tt.dtdelements, to.dtdelements, to.count, "dtdelements", to.dtdq0, so.jac_init)
+
+
+def test_full_length_requests_and_latency_record():
+    """Two full C0 requests (2000 steps) in the mix with short ones; latency fields are consistent."""
+    el, h, tmax = W.plain_3body(0)
+    longs = []
+    for _ in range(2):
+        ic = W.ic_of(el)
+        longs.append((nbg.State(ic), nbg.TransitTiming(tmax, ic), nbg.Integrator(nbg.ahl21, h, 0.0, tmax), True))
+    reqs = longs + make_requests(6, seed=3)
+    with nbg.Server(slots_per_group=64) as srv:
+        mix, infos = serve_mix(srv, reqs, seed=2)
+    for inf in infos:
+        assert inf["latency_ms"] >= inf["run_ms"] >= 0.0 and inf["queue_ms"] >= 0.0
+        assert abs(inf["latency_ms"] - inf["queue_ms"] - inf["run_ms"]) < 1e-6 * max(1.0, inf["latency_ms"]) + 1e-3
+    assert infos[0]["nsteps"] == 2000
+    s, tt = mix[0]
+    assert tt.count.sum() > 100
+    # the same request through nbg_integrate_transits
+    s1, tt1, intr, _ = fresh(reqs[0])
+    intr(s1, tt1, grad=True)
+    assert_same((s, tt), (s1, tt1))
+
+
+def test_errors_and_cancellation():
+    with nbg.Server(slots_per_group=32) as srv:
+        el, h, tmax = W.plain_3body(1)
+        ic = W.ic_of(el)
+        s = nbg.State(ic)
+        tt = nbg.TransitTiming(tmax, ic)
+        tt.count[0] = 1
+        with pytest.raises(ValueError):
+            srv.submit(s, tt, nbg.Integrator(nbg.ahl21, h, 0.0, tmax))
+        with pytest.raises(nbg.NbgError):
+            srv.result(123456, s, tt, timeout_ms=0)
+        with pytest.raises(nbg.NbgError) as ei:
+            srv.wait_any(timeout_ms=10)
+        assert ei.value.code == nbg._lib.NBG_ETIMEOUT
