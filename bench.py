@@ -347,6 +347,8 @@ def main():
     ap.add_argument("--kernel-timing", default="timed", choices=["timed", "separate"],
                     help="CUDA-event pairs around each kernel inside the timed steps, or in one extra pass")
     ap.add_argument("--spw", type=int, default=0, help="orbit producer systems per warp (0 = automatic)")
+    ap.add_argument("--orbit-team", type=int, default=-1,
+                    help="orbit producer form: -1 automatic, 0 one lane per system, 1 a team per system")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--e2e-steps", type=int, default=2)
@@ -386,6 +388,7 @@ def main():
     chunk = args.chunk or 64  # the library's default chunk length (not shortened at these sizes)
     if args.spw:
         ctx.set_orbit_lanes(args.spw)
+    ctx.set_orbit_team(args.orbit_team)
     states, timings, hs, tms, nsteps = build_workload(nbg, args.workload, args.nsys, replica_seed(args.seed, rank))
     total_ss = int(sum(nsteps))
     b = make_batch(nbg, states, timings, hs, tms)
@@ -482,6 +485,7 @@ def main():
                        "grad": True, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "working set larger than L2 (operator records + jac_step)",
                        "chunk_steps": chunk, "orbit_systems_per_warp": args.spw or "auto",
+                       "orbit_team": {-1: "auto", 0: "off", 1: "on"}[args.orbit_team],
                        "streams": 1 if args.serial else 3},
             "e2e": {"value": e2e_val, "unit": "system-steps/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.mean(e2e_ms)) if e2e_ms else None},

@@ -194,6 +194,9 @@ typedef struct {
   int32_t max_inflight;      /* chunks a group may have queued on the GPU; 0 = 2          */
   int32_t orbit_lanes;       /* orbit producer systems per warp (1..32); 0 = 32           */
   uint64_t hbm_budget_bytes; /* device memory the server may hold; 0 = a quarter of free  */
+  int32_t orbit_team;        /* -1 or 0 (the zero-initialised default) = automatic; see
+                                nbg_set_orbit_team (1: always, -2 never)              */
+  int32_t reserved;
 } nbg_server_config;
 
 typedef struct {
@@ -264,6 +267,15 @@ int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double
 /* Systems per warp of the orbit producer (1..32; 0 = automatic: about two
  * warps per SM).  A tuning knob; results do not depend on it. */
 int nbg_set_orbit_lanes(nbg_context* ctx, int systems_per_warp);
+
+/* Form of the orbit producer for groups without kick pairs: -1 automatic
+ * (default: a team of N/2 lanes per system from N = 5 on), 0 one lane per
+ * system, 1 a team for every N.  A team runs the Kepler sweeps and
+ * phisalpha!'s pair loops level by level (pairs with equal i + j share no
+ * body and run in parallel), which keeps every body's sequence of updates
+ * and so gives bitwise the same results.  A tuning knob; no counterpart in
+ * the reference. */
+int nbg_set_orbit_team(nbg_context* ctx, int mode);
 
 /* Record an event pair around every orbit / Jacobian launch (off by default). */
 int nbg_set_profiling(nbg_context* ctx, int on);

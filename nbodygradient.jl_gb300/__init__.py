@@ -281,11 +281,11 @@ class Server:
     """
 
     def __init__(self, device=0, slots_per_group=0, chunk_steps=0, max_inflight=0, orbit_lanes=0,
-                 hbm_budget_bytes=0):
+                 hbm_budget_bytes=0, orbit_team=0):
         import ctypes
         L = _lib.load()
         cfg = _lib.ServerConfig(int(slots_per_group), int(chunk_steps), int(max_inflight), int(orbit_lanes),
-                                int(hbm_budget_bytes))
+                                int(hbm_budget_bytes), int(orbit_team), 0)
         h = ctypes.c_void_p()
         _lib.check(L.nbg_server_start(int(device), ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h

@@ -31,7 +31,7 @@ EXPORTS = (
     "nbg_create", "nbg_destroy", "nbg_last_error", "nbg_version", "nbg_device_info",
     "nbg_integrate_transits", "nbg_batch_integrate_transits", "nbg_batch_integrate_transits_device",
     "nbg_set_tuning", "nbg_last_timing", "nbg_last_launch_count", "nbg_fp64_peak",
-    "nbg_set_profiling", "nbg_last_kernel_stats", "nbg_set_orbit_lanes",
+    "nbg_set_profiling", "nbg_last_kernel_stats", "nbg_set_orbit_lanes", "nbg_set_orbit_team",
     "nbg_batch_integrate_transits_noalloc",
     "nbg_server_start", "nbg_server_enqueue", "nbg_server_wait_any", "nbg_server_poll", "nbg_server_stats",
     "nbg_server_stop",
@@ -58,7 +58,7 @@ class DeviceInfo(ctypes.Structure):
 class ServerConfig(ctypes.Structure):
     _fields_ = [("slots_per_group", ctypes.c_int32), ("chunk_steps", ctypes.c_int32),
                 ("max_inflight", ctypes.c_int32), ("orbit_lanes", ctypes.c_int32),
-                ("hbm_budget_bytes", ctypes.c_uint64)]
+                ("hbm_budget_bytes", ctypes.c_uint64), ("orbit_team", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class RequestInfo(ctypes.Structure):
@@ -119,6 +119,7 @@ def load(build_if_missing=True):
     L.nbg_fp64_peak.argtypes = [_VP, _D]
     L.nbg_set_profiling.argtypes = [_VP, ctypes.c_int]
     L.nbg_set_orbit_lanes.argtypes = [_VP, ctypes.c_int]
+    L.nbg_set_orbit_team.argtypes = [_VP, ctypes.c_int]
     L.nbg_last_kernel_stats.argtypes = [_VP, _I64, _I64]
     L.nbg_server_start.argtypes = [ctypes.c_int, ctypes.POINTER(ServerConfig), ctypes.POINTER(_VP)]
     L.nbg_server_enqueue.argtypes = [_VP, ctypes.POINTER(SystemDesc), ctypes.c_double, _D, _D, _D, _D, _D, _D, _D,
@@ -191,6 +192,10 @@ class Context:
 
     def set_orbit_lanes(self, systems_per_warp=0):
         check(load().nbg_set_orbit_lanes(self._h, int(systems_per_warp)))
+
+    def set_orbit_team(self, mode=-1):
+        """-1 automatic, 0 one lane per system, 1 a team of lanes per system."""
+        check(load().nbg_set_orbit_team(self._h, int(mode)))
 
     def set_profiling(self, on=True):
         check(load().nbg_set_profiling(self._h, int(bool(on))))

@@ -224,14 +224,16 @@ struct nbg_context {
   int chunk_steps = 64;
   int overlap = 1;  // orbit producer on its own stream, one chunk ahead of the rest
   int orbit_spw = 0;  // 0: automatic
+  int orbit_team = -1;  // -1: automatic (teams for N >= 5), 0: one lane per system, 1: teams for every N
   int sm_count = 0;
   double last_total_ms = 0, last_orbit_ms = 0, last_jac_ms = 0, last_transit_ms = 0, last_ops_ms = 0;
   long long last_launches = 0, last_orbit_launches = 0, last_jac_launches = 0;
   int profile = 0;
   std::vector<cudaEvent_t> prof_events;  // pairs around each timed launch
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaStream_t stream_w = nullptr;       // operator / Jacobian stream (overlap mode)
-  cudaStream_t stream_t = nullptr;       // transit-search stream (overlap mode)
+  // overlap mode: per group q, a producer stream, an operator / Jacobian
+  // stream and a transit-search stream (gstreams[3q .. 3q+2])
+  std::vector<cudaStream_t> gstreams;
   std::vector<cudaEvent_t> sync_events;  // cross-stream ordering, no timing
 
   int sync_event(size_t i, cudaEvent_t* out) {
@@ -306,6 +308,20 @@ int launch_group_transit(int N, const GroupArgs& g, int chunk, cudaStream_t st) 
 int launch_group_operators(int N, const GroupArgs& g, int chunk, cudaStream_t st) { return kOps[N](g, chunk, st); }
 int launch_group_jacobian(int N, const GroupArgs& g, int chunk, cudaStream_t st) { return kJac[N](g, chunk, st); }
 int launch_group_seed(int N, const GroupArgs& g, cudaStream_t st) { return kSeed[N](g, st); }
+}  // namespace nbg
+
+namespace {
+
+}  // namespace
+
+namespace nbg {
+// Team producer (a team of lanes per system) for kick-free groups: automatic
+// from five bodies on, where the level-parallel sweeps shorten the step's
+// critical path by 1.4x (N = 5) to 2.6x (N = 10).
+bool use_team(int mode, int N, unsigned long long kick) {
+  if (kick) return false;
+  return mode > 0 || (mode < 0 && N >= 5);
+}
 }  // namespace nbg
 
 namespace {
@@ -410,6 +426,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     // whatever its lane count; with the overlapped streams, full warps leave
     // the most FP64 issue slots to the kernels running beside the producer.
     // Without overlap a small batch is spread over about two warps per SM.
+    g.team = use_team(ctx->orbit_team, N, gp.kick) && ctx->orbit_spw == 0;
     if (ctx->orbit_spw > 0) {
       g.spw = ctx->orbit_spw;
     } else if (ctx->overlap) {
@@ -554,35 +571,40 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
       }
     }
   } else {
-    // Three streams.  st runs the orbit producer, chunk after chunk; once
-    // the producer has finished chunk c, stt runs chunk c's transit searches
-    // while sw runs its operator kernels, and then (after the searches) its
-    // Jacobian consumer.  Chunk c + 2 reuses chunk c's buffer half, so the
-    // producer waits for chunk c's consumer before it starts chunk c + 2.
-    // The producer thus runs one chunk ahead, and the latency-bound producer
-    // and search warps share the SMs with the throughput-bound operator and
-    // Jacobian kernels.
-    if (!ctx->stream_w) NBG_CUDA(cudaStreamCreateWithFlags(&ctx->stream_w, cudaStreamNonBlocking));
-    if (!ctx->stream_t) NBG_CUDA(cudaStreamCreateWithFlags(&ctx->stream_t, cudaStreamNonBlocking));
-    cudaStream_t sw = ctx->stream_w, stt = ctx->stream_t;
-    cudaEvent_t evs, evt_join;
+    // Three streams per group.  sp runs the group's orbit producer, chunk
+    // after chunk; once the producer has finished chunk c, stt runs chunk
+    // c's transit searches while sw runs its operator kernels, and then
+    // (after the searches) its Jacobian consumer.  Chunk c + 2 reuses chunk
+    // c's buffer half, so the producer waits for chunk c's consumer before it
+    // starts chunk c + 2.  The producer thus runs one chunk ahead, and the
+    // latency-bound producer and search warps share the SMs with the
+    // throughput-bound operator and Jacobian kernels.  With a stream triple of
+    // its own, every group (body count, grad, pair pattern) progresses
+    // independently: its chunk chain is not held up by another group's.
+    const size_t ng = gargs.size();
+    while (ctx->gstreams.size() < 3 * ng) {
+      cudaStream_t s2;
+      NBG_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+      ctx->gstreams.push_back(s2);
+    }
+    cudaEvent_t evs;
     if ((rc = ctx->sync_event(0, &evs))) return rc;
     NBG_CUDA(cudaEventRecord(evs, st));
-    NBG_CUDA(cudaStreamWaitEvent(sw, evs, 0));  // sw and stt start after the packing on st
-    NBG_CUDA(cudaStreamWaitEvent(stt, evs, 0));
+    for (size_t q = 0; q < 3 * ng; q++) NBG_CUDA(cudaStreamWaitEvent(ctx->gstreams[q], evs, 0));  // after the packing
     for (long long c = 0; c < nchunks; c++) {
-      for (size_t q = 0; q < gargs.size(); q++) {
+      for (size_t q = 0; q < ng; q++) {
         if (c * K >= gmaxsteps[q]) continue;
         const int par = (int)(c & 1);
         const GroupArgs& g = par ? ghalf[q] : gargs[q];
+        cudaStream_t sp = ctx->gstreams[3 * q], sw = ctx->gstreams[3 * q + 1], stt = ctx->gstreams[3 * q + 2];
         cudaEvent_t ev_orb, ev_done, ev_tr;
         if ((rc = ctx->sync_event(2 + 6 * q + par, &ev_orb)) || (rc = ctx->sync_event(4 + 6 * q + par, &ev_done)) ||
             (rc = ctx->sync_event(6 + 6 * q + par, &ev_tr)))
           return rc;
-        if (c >= 2) NBG_CUDA(cudaStreamWaitEvent(st, ev_done, 0));
-        NBG_CUDA(cudaMemsetAsync(g.task_count, 0, sizeof(int), st));
-        if ((rc = timed(0, [&] { return kOrbit[g.N](g, (int)c, st); }))) return rc;
-        NBG_CUDA(cudaEventRecord(ev_orb, st));
+        if (c >= 2) NBG_CUDA(cudaStreamWaitEvent(sp, ev_done, 0));
+        NBG_CUDA(cudaMemsetAsync(g.task_count, 0, sizeof(int), sp));
+        if ((rc = timed_on(sp, 0, [&] { return kOrbit[g.N](g, (int)c, sp); }))) return rc;
+        NBG_CUDA(cudaEventRecord(ev_orb, sp));
         NBG_CUDA(cudaStreamWaitEvent(stt, ev_orb, 0));
         NBG_CUDA(cudaStreamWaitEvent(sw, ev_orb, 0));
         if ((rc = timed_on(stt, 2, [&] { return kTransit[g.N](g, (int)c, stt); }))) return rc;
@@ -601,11 +623,14 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
         NBG_CUDA(cudaEventRecord(ev_done, sw));
       }
     }
-    if ((rc = ctx->sync_event(1, &evt_join))) return rc;
-    NBG_CUDA(cudaEventRecord(evs, sw));
-    NBG_CUDA(cudaEventRecord(evt_join, stt));
-    NBG_CUDA(cudaStreamWaitEvent(st, evs, 0));  // join: everything after runs on st
-    NBG_CUDA(cudaStreamWaitEvent(st, evt_join, 0));
+    // join: everything after runs on st (an event recorded on a stream and
+    // waited on at once may be re-recorded for the next stream)
+    for (size_t q = 0; q < 3 * ng; q++) {
+      cudaEvent_t ej;
+      if ((rc = ctx->sync_event(1, &ej))) return rc;
+      NBG_CUDA(cudaEventRecord(ej, ctx->gstreams[q]));
+      NBG_CUDA(cudaStreamWaitEvent(st, ej, 0));
+    }
   }
   NBG_CUDA(cudaGetLastError());
   NBG_CUDA(cudaEventRecord(ctx->ev1, st));
@@ -1043,11 +1068,10 @@ int nbg_destroy(nbg_context* ctx) {
   cudaEventDestroy(ctx->ev1);
   for (auto e : ctx->prof_events) cudaEventDestroy(e);
   for (auto e : ctx->sync_events) cudaEventDestroy(e);
-  for (cudaStream_t s2 : {ctx->stream_w, ctx->stream_t})
-    if (s2) {
-      cudaStreamSynchronize(s2);
-      cudaStreamDestroy(s2);
-    }
+  for (cudaStream_t s2 : ctx->gstreams) {
+    cudaStreamSynchronize(s2);
+    cudaStreamDestroy(s2);
+  }
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return NBG_OK;
@@ -1066,6 +1090,13 @@ int nbg_set_orbit_lanes(nbg_context* ctx, int systems_per_warp) {
   if (systems_per_warp < 0 || systems_per_warp > 32)
     return set_error(NBG_EINVAL, "systems_per_warp = %d not in 0..32", systems_per_warp);
   ctx->orbit_spw = systems_per_warp;
+  return NBG_OK;
+}
+
+int nbg_set_orbit_team(nbg_context* ctx, int mode) {
+  if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
+  if (mode < -1 || mode > 1) return set_error(NBG_EINVAL, "mode = %d not in -1..1", mode);
+  ctx->orbit_team = mode;
   return NBG_OK;
 }
 

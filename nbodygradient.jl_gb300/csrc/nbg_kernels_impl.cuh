@@ -14,6 +14,7 @@
 #pragma once
 #include "../../include/nbg.h"
 #include "nbg_jacobian.cuh"
+#include "nbg_orbit_team.cuh"
 
 namespace nbg {
 
@@ -330,6 +331,11 @@ __global__ void seed_gsave_kernel(GroupArgs g) {
 
 template <int N>
 int launch_orbit(const GroupArgs& g, int chunk, cudaStream_t st) {
+  if (g.team && !g.kick) {
+    constexpr int T = PROD_BS / team_lanes(N);
+    orbit_team_kernel<N><<<(g.S + T - 1) / T, PROD_BS, 0, st>>>(g, chunk);
+    return 0;
+  }
   int blocks = (g.S + g.spw - 1) / g.spw;
   orbit_chunk_kernel<N><<<blocks, PROD_BS, 0, st>>>(g, chunk);
   return 0;

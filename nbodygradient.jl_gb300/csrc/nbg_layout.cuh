@@ -36,7 +36,8 @@ __host__ __device__ inline int snap_count(bool kick) { return kick ? 3 : 1; }
 
 struct GroupArgs {
   int N, S, nsys, grad, K, R, npk;
-  int spw;  // orbit producer: systems per warp (lanes >= spw idle)
+  int spw;   // orbit producer: systems per warp (lanes >= spw idle)
+  int team;  // orbit producer: 1 = a team of lanes per system (orbit_team_kernel), 0 = one lane
   unsigned long long kick;
   // per-system state, structure of arrays: element e of system s at [e * S + s]
   double *x, *v, *xe, *ve, *m, *dqdt, *gsave;

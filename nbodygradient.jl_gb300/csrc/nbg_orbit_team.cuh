@@ -1,0 +1,236 @@
+// nbg_orbit_team.cuh -- the orbit producer with a team of lanes per system.
+//
+// The Kepler sweeps of an AHL21 step (ahl21.jl:25-27 forward, :56-58
+// backward) update bodies i and j of each pair in a fixed order.  A pair's
+// update reads and writes only x, v (and their Kahan errors) of its two
+// bodies, so two pairs with no body in common commute exactly.  In the
+// forward order (i = 0..N-2, j = i+1..N-1), the pairs that touch body b come
+// in order of increasing i + j: (0,b), (1,b), ..., (b-1,b), (b,b+1), ...,
+// (b,N-1).  The pairs with one value of i + j share no body.  Running the
+// sweep "level by level" in increasing i + j, with the pairs of one level
+// in parallel, therefore applies to every body the same updates in the same
+// order as the sequential sweep: the result is bitwise identical.  The
+// backward sweep is the exact reverse sequence, so it runs the levels in
+// decreasing i + j.  phisalpha!'s two pair loops (the acceleration sums and
+// the velocity kicks, ahl21.jl:558-700 without the gradient) follow the same
+// pair order and run level by level too.
+//
+// A level holds at most floor(N/2) pairs, so a team of L = max(1, N/2) lanes
+// runs one system, 32 / L systems per warp, the system's x, v, errors and
+// masses in shared memory.  The critical path of a sweep drops from
+// N(N-1)/2 to 2N-3 pair solves (N = 10: 45 -> 17; N = 8: 28 -> 13).
+//
+// Groups with kick pairs (pair[i,j] == true) keep the one-lane producer.
+// The last step of a grad system (which also forms dq/dt, the State's
+// output) runs the one-lane step on the team's first lane.
+#pragma once
+#include "nbg_orbit.cuh"
+
+namespace nbg {
+
+__host__ __device__ constexpr int team_lanes(int N) { return N / 2 > 1 ? N / 2 : 1; }
+
+// phisalpha!, first pair loop (accelerations), for one pair; the same
+// operations in the same order as phisalpha<N, false>.
+template <int N>
+__device__ __forceinline__ void phis_accel_pair(const Sys<N>& s, double* a, int i, int j) {
+  double rij[3];
+  for (int k = 0; k < 3; k++) rij[k] = s.x[3 * i + k] - s.x[3 * j + k];
+  double r2 = rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2];
+  double r3 = r2 * sqrt(r2);
+  double fac2 = GNEWT / r3;
+  for (int k = 0; k < 3; k++) {
+    double fac = fac2 * rij[k];
+    a[3 * i + k] = a[3 * i + k] - s.m[j] * fac;
+    a[3 * j + k] = a[3 * j + k] + s.m[i] * fac;
+  }
+}
+
+// phisalpha!, second pair loop (velocity corrections), for one pair.
+template <int N>
+__device__ __forceinline__ void phis_kick_pair(Sys<N>& s, const double* a, int i, int j, double coeff) {
+  double rij[3], aij[3];
+  for (int k = 0; k < 3; k++) {
+    aij[k] = a[3 * i + k] - a[3 * j + k];
+    rij[k] = s.x[3 * i + k] - s.x[3 * j + k];
+  }
+  double r2 = rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2];
+  double r1 = sqrt(r2);
+  double ardot = aij[0] * rij[0] + aij[1] * rij[1] + aij[2] * rij[2];
+  double fac1 = coeff / (r2 * r2 * r1);
+  double mij = s.m[i] + s.m[j];
+  double fac2 = 2.0 * GNEWT * mij / r1 + 3.0 * ardot;
+  for (int k = 0; k < 3; k++) {
+    double fac = fac1 * (rij[k] * fac2 - r2 * aij[k]);
+    kahan(s.v[3 * i + k], s.ve[3 * i + k], s.m[j] * fac);
+    kahan(s.v[3 * j + k], s.ve[3 * j + k], (-s.m[i]) * fac);
+  }
+}
+
+// The pair of level `lev` (i + j == lev) that lane t of a team takes, if any.
+template <int N>
+__device__ __forceinline__ bool level_pair(int lev, int t, int* i, int* j) {
+  const int imin = lev - (N - 1) > 0 ? lev - (N - 1) : 0;
+  const int ii = imin + t;
+  if (2 * ii >= lev) return false;  // i < j = lev - i
+  *i = ii;
+  *j = lev - ii;
+  return true;
+}
+
+// One AHL21 step without gradient operators for a group with no kick pairs
+// (ahl21_no_grad.jl:6-18 order), run by the L lanes of a team; `run` is false
+// for lanes whose system does not step (they still meet every __syncwarp).
+// cap / xs as in ahl21_step.  a: the team's 3N acceleration scratch.
+template <int N>
+__device__ __forceinline__ void team_step(Sys<N>& s, double* a, Work<N>& w, int t, bool run, double h,
+                                          const Rec& cap, const Rec& xs) {
+  constexpr int L = team_lanes(N);
+  constexpr int P = N * (N - 1) / 2;
+  const double h2 = 0.5 * h;
+  if (run)
+    for (int q = t; q < 3 * N; q += L) kahan(s.x[q], s.xe[q], h2 * s.v[q]);
+  __syncwarp();
+  for (int lev = 1; lev <= 2 * N - 3; lev++) {
+    int i, j;
+    if (run && level_pair<N>(lev, t, &i, &j))
+      kepler_pair<N, true, false, false>(s, w, i, j, h2, Rec{nullptr, 0}, 0, cap, pair_bit(i, j, N) * PCAP);
+    __syncwarp();
+  }
+  if (run) {
+    if (xs.p)
+      for (int q = t; q < 3 * N; q += L) xs.put(q, s.x[q]);
+    for (int q = t; q < 3 * N; q += L) a[q] = 0.0;
+  }
+  __syncwarp();
+  const double coeff = 2.0 * (h * h * h) / 96.0 * 2.0 * GNEWT;  // alpha = 2 (ahl21.jl:47)
+  for (int lev = 1; lev <= 2 * N - 3; lev++) {
+    int i, j;
+    if (run && level_pair<N>(lev, t, &i, &j)) phis_accel_pair<N>(s, a, i, j);
+    __syncwarp();
+  }
+  for (int lev = 1; lev <= 2 * N - 3; lev++) {
+    int i, j;
+    if (run && level_pair<N>(lev, t, &i, &j)) phis_kick_pair<N>(s, a, i, j, coeff);
+    __syncwarp();
+  }
+  for (int lev = 2 * N - 3; lev >= 1; lev--) {
+    int i, j;
+    if (run && level_pair<N>(lev, t, &i, &j))
+      kepler_pair<N, false, false, false>(s, w, i, j, h2, Rec{nullptr, 0}, 0, cap,
+                                          (P + (P - 1 - pair_bit(i, j, N))) * PCAP);
+    __syncwarp();
+  }
+  if (run)
+    for (int q = t; q < 3 * N; q += L) kahan(s.x[q], s.xe[q], h2 * s.v[q]);
+  __syncwarp();
+}
+
+// Orbit producer, team form: L lanes per system, T = 32 / L systems per warp
+// (lanes beyond T * L idle).  Same inputs, outputs and arithmetic as
+// orbit_chunk_kernel<N> for groups without kick pairs.
+template <int N>
+__global__ void __launch_bounds__(PROD_BS) orbit_team_kernel(GroupArgs g, int chunk) {
+  constexpr int L = team_lanes(N);
+  constexpr int T = PROD_BS / L;
+  __shared__ Sys<N> sys[T];
+  __shared__ double acc[T][3 * N];
+  __shared__ double gsv[T][N];
+  __shared__ long long cnt[T][N];
+  const int lane = threadIdx.x;
+  const int team = lane / L, t = lane % L;
+  const bool in_team = team < T;
+  const int tm = in_team ? team : 0;  // idle lanes alias team 0 but never write
+  const int s = blockIdx.x * T + tm;
+  const int S = g.S;
+  bool valid = in_team && s < S && g.sysidx[s] >= 0;
+  const long long nst = valid ? g.nsteps[s] : 0;
+  const long long k0 = valid ? chunk_first_step(g, chunk, s) : 0;
+  if (k0 >= nst) valid = false;
+  Sys<N>& st = sys[tm];
+  if (valid) {
+    for (int q = t; q < 3 * N; q += L) {
+      st.x[q] = g.x[q * S + s];
+      st.v[q] = g.v[q * S + s];
+      st.xe[q] = g.xe[q * S + s];
+      st.ve[q] = g.ve[q * S + s];
+    }
+    for (int q = t; q < N; q += L) {
+      st.m[q] = g.m[q * S + s];
+      gsv[tm][q] = g.gsave[q * S + s];
+      cnt[tm][q] = g.count[q * S + s];
+    }
+    for (int q = t; q < 7 * N; q += L) st.dqdt[q] = g.dqdt[q * S + s];
+  }
+  __syncwarp();
+  Work<N> w;
+  const double t0 = valid ? g.t0[s] : 0.0, h = valid ? g.h[s] : 0.0, hI = valid ? g.hI[s] : 0.0;
+  const int ntt = valid ? g.ntt[s] : 0, ti = valid ? g.ti[s] : 0;
+  for (int kk = 0; kk < g.K; kk++) {
+    const long long istep = k0 + kk;
+    const bool run = valid && istep < nst;
+    if (!__any_sync(0xffffffffu, run)) break;
+    const bool last = run && g.grad && istep == nst - 1;
+    Rec cap{nullptr, 0}, xs{nullptr, 0};
+    if (g.grad) {
+      cap = Rec{g.pcap + (size_t)kk * 2 * g.npk * PCAP * S + s, S};
+      xs = Rec{g.xsnap + (size_t)kk * snap_count(false) * 3 * N * S + s, S};
+    }
+    team_step<N>(st, acc[tm], w, t, run && !last, h, cap, xs);
+    // the last step also forms dq/dt: the one-lane step, on the team's first lane
+    if (last && t == 0) ahl21_step<N, true, true>(st, w, h, 0, Rec{nullptr, 0}, cap, xs);
+    __syncwarp();
+    // detect_transits! (timing.jl:3-28); occultor o on lane o % L
+    if (run) {
+      const double tnow = t0 + (double)(istep + 1) * h;
+      for (int o = t; o < N - 1; o += L) {
+        const int ib = (o < ti) ? o : o + 1;
+        const double gi = gsky(st, ib, ti);
+        const double xi = st.x[3 * ib], yi = st.x[3 * ib + 1], zi = st.x[3 * ib + 2];
+        const double ri = sqrt(xi * xi + yi * yi + zi * zi);
+        if (g.grad) g.tflag[(size_t)(kk * (N - 1) + o) * S + s] = -1;
+        if (gi > 0.0 && gsv[tm][ib] < 0.0 && -zi > 0.25 * ri && ri < 1e12) {
+          cnt[tm][ib] += 1;
+          if (cnt[tm][ib] <= ntt) {
+            const int idx = atomicAdd(g.task_count, 1);
+            if (idx < g.task_cap) {
+              double* tf = g.task_f + (size_t)idx * (12 * N + 2);
+              for (int q = 0; q < 3 * N; q++) {
+                tf[q] = st.x[q];
+                tf[3 * N + q] = st.v[q];
+                tf[6 * N + q] = st.xe[q];
+                tf[9 * N + q] = st.ve[q];
+              }
+              tf[12 * N] = -gi * hI / (gi - gsv[tm][ib]);  // first estimate (timing.jl:20)
+              tf[12 * N + 1] = tnow;
+              int* tk = g.task_i + 3 * idx;
+              tk[0] = s;
+              tk[1] = kk * (N - 1) + o;
+              tk[2] = (int)(cnt[tm][ib] - 1);
+            }
+          } else {
+            atomicOr(g.status + s, NBG_STATUS_NTT_OVERFLOW);
+          }
+        }
+        gsv[tm][ib] = gi;
+      }
+    }
+    __syncwarp();
+  }
+  if (valid) {
+    for (int q = t; q < 3 * N; q += L) {
+      g.x[q * S + s] = st.x[q];
+      g.v[q * S + s] = st.v[q];
+      g.xe[q * S + s] = st.xe[q];
+      g.ve[q * S + s] = st.ve[q];
+    }
+    if (g.grad && nst <= k0 + g.K)
+      for (int q = t; q < 7 * N; q += L) g.dqdt[q * S + s] = st.dqdt[q];
+    for (int q = t; q < N; q += L) {
+      g.gsave[q * S + s] = gsv[tm][q];
+      g.count[q * S + s] = cnt[tm][q];
+    }
+  }
+}
+
+}  // namespace nbg

@@ -296,6 +296,7 @@ int create_group(nbg_server* srv, int N, int grad, unsigned long long kick, Grou
   memset(&g, 0, sizeof(g));
   g.N = N; g.S = C; g.nsys = C; g.grad = grad; g.K = K; g.kick = kick; g.npk = npk;
   g.spw = srv->cfg.orbit_lanes;
+  g.team = use_team(srv->cfg.orbit_team, N, kick);
   g.R = step_record_size(N, npk, kick != 0);
   g.task_cap = K * (N - 1) * C;
   g.tgrid = std::min(((g.task_cap + 31) / 32) * 32, std::max(1, srv->sm_count) * 4 * 32);
@@ -677,6 +678,8 @@ int nbg_server_start(int device, const nbg_server_config* cfg_in, nbg_server** o
   if (!cfg.chunk_steps) cfg.chunk_steps = 32;
   if (!cfg.max_inflight) cfg.max_inflight = 2;
   if (!cfg.orbit_lanes) cfg.orbit_lanes = 32;
+  if (cfg.orbit_team < -2 || cfg.orbit_team > 1) return set_error(NBG_EINVAL, "orbit_team = %d", cfg.orbit_team);
+  cfg.orbit_team = cfg.orbit_team == 0 ? -1 : (cfg.orbit_team == -2 ? 0 : cfg.orbit_team);  // use_team's modes
   if (!cfg.hbm_budget_bytes) {
     size_t fr = 0, tot = 0;
     NBG_CUDA(cudaMemGetInfo(&fr, &tot));

@@ -205,3 +205,28 @@ def test_batch_matches_oracle():
         to = O.OTiming(states[q].n, timings[q].ntt, 0)
         O.integrate_transits(so, to, h, tmax)
         compare(gs[q], timings[q], so, to, tmax)
+
+
+@pytest.mark.parametrize("grad", [True, False])
+def test_team_producer_is_bitwise_the_one_lane_producer(grad):
+    """The team form of the orbit producer (level-parallel sweeps) against the
+    one-lane form, for every body count: bitwise the same x, v, jac_step,
+    transit times and derivatives."""
+    specs = []
+    for n in range(2, 11):
+        els, hs, tms = W.batch_uneven(3, seed=40 + n, nmin=n, nmax=n)
+        specs += [(el, h, 90 * h, grad) for el, h in zip(els, hs)]
+    states, timings, hs, tms, grads = _batch_inputs(specs)
+    out = []
+    for mode in (0, 1):
+        ctx = nbg.Context(0)
+        ctx.set_orbit_team(mode)
+        b = nbg.Batch([s.n for s in states], 0, hs, tms, [t.ntt for t in timings], grads)
+        for q in range(len(states)):
+            b.set_system(q, states[q], timings[q])
+        b.run(ctx)
+        out.append(b)
+        ctx.close()
+    assert sum(int(c) for c in out[0].arrays["count"]) > 0
+    for k in ("x", "v", "xerror", "verror", "tt", "count", "jac_step", "jac_error", "dtdq0", "dtdelements", "dqdt"):
+        assert np.array_equal(out[0].arrays[k], out[1].arrays[k]), k
