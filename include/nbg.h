@@ -96,6 +96,29 @@ int nbg_integrate_transits(nbg_context* ctx, int n, int ti, double h, double tma
                            int64_t* count);
 
 /*
+ * (intr::Integrator)(s::State{Float64}, time::Float64; grad)
+ * Replaces src/integrator/Integrator.jl:159-197 with intr.scheme === ahl21!:
+ * nsteps = |round((time - s.t)/h)| steps of h * check_step(s.t, time), then,
+ * when tmax = s.t + h nsteps differs from time, one step of time - tmax; s.t
+ * is set to time.  x, v, xerror, verror, jac_step, jac_error and dqdt are
+ * updated in place (jac_step / jac_error / dqdt only with grad; dqdt is that
+ * of the last step, as in the reference).  intr(s; grad) (Integrator.jl:247)
+ * is this call with time = s.t + intr.tmax.
+ */
+int nbg_integrate(nbg_context* ctx, int n, double h, double time, int grad, double* t, double* x, double* v,
+                  const double* m, double* xerror, double* verror, double* jac_step, double* jac_error, double* dqdt,
+                  const uint8_t* pair);
+
+/*
+ * (intr::Integrator)(s::State{Float64}, N::Int64; grad)
+ * Replaces src/integrator/Integrator.jl:210-233: |N| steps of h (of -h when
+ * N < 0); s.t advances by the compensated sum of the signed steps.
+ */
+int nbg_integrate_steps(nbg_context* ctx, int n, double h, int64_t nsteps, int grad, double* t, double* x,
+                        double* v, const double* m, double* xerror, double* verror, double* jac_step,
+                        double* jac_error, double* dqdt, const uint8_t* pair);
+
+/*
  * Batched form: nsys independent systems integrated in one plan.  Each
  * system's arrays are laid out exactly as for nbg_integrate_transits and
  * concatenated system after system in every packed buffer (so the offset of
@@ -118,6 +141,17 @@ int nbg_batch_integrate_transits(nbg_context* ctx, int nsys, const nbg_system_de
                                  double* v, const double* m, double* xerror, double* verror, double* jac_step,
                                  double* jac_error, double* dqdt, const uint8_t* pair, const double* jac_init,
                                  double* tt, double* dtdq0, double* dtdelements, int64_t* count, uint32_t* status);
+
+/*
+ * nbg_integrate for nsys systems in one plan: desc[s].tmax is system s's
+ * target time (the `time` of intr(s, time)), desc[s].h its step and
+ * desc[s].grad its flag (ti and ntt are ignored); arrays packed as for
+ * nbg_batch_integrate_transits.  No reference counterpart (the reference
+ * loops in Julia).
+ */
+int nbg_batch_integrate(nbg_context* ctx, int nsys, const nbg_system_desc* desc, double* t, double* x, double* v,
+                        const double* m, double* xerror, double* verror, double* jac_step, double* jac_error,
+                        double* dqdt, const uint8_t* pair);
 
 /*
  * Same as nbg_batch_integrate_transits, but every array pointer (and desc)

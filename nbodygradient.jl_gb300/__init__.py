@@ -132,12 +132,25 @@ class Integrator:
         self.h, self.t0, self.tmax = float(h), float(t0), float(tmax)
 
     def __call__(self, s, tt=None, grad=True, ctx=None):
-        if tt is None or not isinstance(tt, TransitTiming):
-            raise NbgError(_lib.NBG_EUNSUPPORTED,
-                           "this build implements intr(s, tt::TransitTiming; grad) on the GPU")
+        """intr(s, tt::TransitTiming; grad)   Transits.jl:173  (transit times)
+        intr(s, time::float; grad)          Integrator.jl:159 (integrate to time)
+        intr(s, N::int; grad)               Integrator.jl:210 (N steps)
+        intr(s; grad)                       Integrator.jl:247 (to s.t + tmax)"""
         ctx = ctx or default_context()
         L = _lib.load()
         p = _lib.ptr
+        if tt is None or isinstance(tt, (float, np.floating, int, np.integer)):
+            args = (p(s.t), p(s.x), p(s.v), p(s.m), p(s.xerror), p(s.verror), p(s.jac_step), p(s.jac_error),
+                    p(s.dqdt), p(s.pair, _lib._U8))
+            if tt is None:
+                tt = float(s.t[0] + self.tmax)
+            if isinstance(tt, (int, np.integer)) and not isinstance(tt, bool):
+                _lib.check(L.nbg_integrate_steps(ctx.handle, s.n, self.h, int(tt), int(bool(grad)), *args))
+            else:
+                _lib.check(L.nbg_integrate(ctx.handle, s.n, self.h, float(tt), int(bool(grad)), *args))
+            return None
+        if not isinstance(tt, TransitTiming):
+            raise NbgError(_lib.NBG_EUNSUPPORTED, "intr(s, tt) takes a TransitTiming, a time or a step count")
         _lib.check(L.nbg_integrate_transits(
             ctx.handle, s.n, tt.ti - 1, self.h, self.tmax, int(bool(grad)), p(s.t), p(s.x), p(s.v), p(s.m),
             p(s.xerror), p(s.verror), p(s.jac_step), p(s.jac_error), p(s.dqdt), p(s.pair, _lib._U8), p(s.jac_init),

@@ -33,6 +33,7 @@ EXPORTS = (
     "nbg_set_tuning", "nbg_last_timing", "nbg_last_launch_count", "nbg_fp64_peak",
     "nbg_set_profiling", "nbg_last_kernel_stats", "nbg_set_orbit_lanes", "nbg_set_orbit_team",
     "nbg_batch_integrate_transits_noalloc",
+    "nbg_integrate", "nbg_integrate_steps", "nbg_batch_integrate",
     "nbg_server_start", "nbg_server_enqueue", "nbg_server_wait_any", "nbg_server_poll", "nbg_server_stats",
     "nbg_server_stop",
 )
@@ -107,6 +108,10 @@ def load(build_if_missing=True):
     L.nbg_integrate_transits.argtypes = [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_int, _D, _D, _D, _D, _D, _D, _D, _D, _D, _U8, _D, ctypes.c_int64,
                                          _D, _D, _D, _I64]
+    plain = [_D, _D, _D, _D, _D, _D, _D, _D, _D, _U8]
+    L.nbg_integrate.argtypes = [_VP, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int] + plain
+    L.nbg_integrate_steps.argtypes = [_VP, ctypes.c_int, ctypes.c_double, ctypes.c_int64, ctypes.c_int] + plain
+    L.nbg_batch_integrate.argtypes = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc)] + plain
     batch_args = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc), _D, _D, _D, _D, _D, _D, _D, _D, _D, _U8, _D, _D, _D,
                   _D, _I64, _U32]
     L.nbg_batch_integrate_transits.argtypes = batch_args

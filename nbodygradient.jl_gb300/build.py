@@ -24,9 +24,11 @@ LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: scalar products and sums round one by one as in Julia; the
-# kernels call fma() where a fused product is meant.
+# kernels call fma() where a fused product is meant.  -ffp-contract=off does
+# the same for the host code (step counts, s.t), which GCC would otherwise
+# contract on AArch64.
 NVCC_FLAGS = ARCH + ["-O3", "--fmad=false", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                     "-I" + INCLUDE]
+                     "-Xcompiler", "-ffp-contract=off", "-I" + INCLUDE]
 BODY_COUNTS = list(range(2, 11))
 
 

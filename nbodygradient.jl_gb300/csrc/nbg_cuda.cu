@@ -326,6 +326,15 @@ bool use_team(int mode, int N, unsigned long long kick) {
 
 namespace {
 
+// A plain integration (no transit timing) of one system: the steps
+// intr(s, time) or intr(s, N) takes (Integrator.jl:159-233).
+struct PlainSpec {
+  long long nsteps;  // steps in all, the fractional last step included
+  double h;          // signed step
+  double hlast;      // length of the last step (h unless it is fractional)
+  double tout;       // s.t after the call
+};
+
 struct GroupPlan {
   int N, grad;
   unsigned long long kick;
@@ -335,10 +344,14 @@ struct GroupPlan {
 
 // Core of every entry point.  All array pointers are device pointers in the
 // caller's packed layout; desc / t0 / pair are host copies.
+// plain: null for transit timing (intr(s, tt)); otherwise one PlainSpec per
+// system, no transit detection and no tt / dtdq0 / dtdelements (those
+// pointers and jac_init may be null; d_count must hold nsys*n zeros).
 int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const double* t_host,
               const uint8_t* pair_host, double* d_t, double* d_x, double* d_v, const double* d_m, double* d_xe,
               double* d_ve, double* d_J, double* d_E, double* d_dqdt, const double* d_jinit, double* d_tt,
-              double* d_dq0, double* d_dtdel, long long* d_count, uint32_t* status_host) {
+              double* d_dq0, double* d_dtdel, long long* d_count, uint32_t* status_host,
+              const PlainSpec* plain = nullptr) {
   cudaStream_t st = ctx->stream;
   ctx->last_launches = 0;
   ctx->last_orbit_ms = ctx->last_jac_ms = ctx->last_transit_ms = ctx->last_ops_ms = 0;
@@ -363,8 +376,13 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     o.n = n; o.ntt = d.ntt; o.grad = d.grad ? 1 : 0; o.pad = 0;
     ax += 3 * n; am += n; aJ += (long long)M * M; adq += M; ap += (long long)n * n;
     att += (long long)n * d.ntt; adq0 += (long long)n * d.ntt * 7 * n; acn += n;
-    nsteps[s] = steps_of(d.h, d.tmax);
-    hsig[s] = d.h * check_step(t_host[s], d.tmax + t_host[s]);
+    if (plain) {
+      nsteps[s] = plain[s].nsteps;
+      hsig[s] = plain[s].h;
+    } else {
+      nsteps[s] = steps_of(d.h, d.tmax);
+      hsig[s] = d.h * check_step(t_host[s], d.tmax + t_host[s]);
+    }
     unsigned long long kick = 0;
     for (int i = 0; i < n - 1; i++)
       for (int j = i + 1; j < n; j++)
@@ -449,6 +467,12 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     GET(x, 3 * N * S); GET(v, 3 * N * S); GET(xe, 3 * N * S); GET(ve, 3 * N * S); GET(m, N * S);
     GET(dqdt, 7 * N * S); GET(gsave, N * S); GET(count, N * S); GET(t0, S); GET(h, S); GET(hI, S);
     GET(nsteps, S); GET(ntt, S); GET(ti, S); GET(sysidx, S); GET(status, S);
+    double* hlast = nullptr;
+    if (plain) {
+      if ((rc = ctx->get(name("hlast"), (size_t)S, &hlast))) return rc;
+      g.hlast = hlast;
+      g.notransit = 1;
+    }
     g.task_cap = K * (N - 1) * S;
     // Per-chunk buffers (the transit queue, the captures and the records) are
     // double-buffered in overlap mode: chunk c uses half c % 2.
@@ -468,13 +492,15 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     g.tt = d_tt; g.off_tt = d_offtt; g.dtdq0 = d_dq0; g.off_dq = d_offdq;
     // host-side scalars
     std::vector<int> sidx(S, -1), vntt(S, 1), vti(S, 0);
-    std::vector<double> vt0(S, 0.0), vh(S, 0.0), vhI(S, 0.0);
+    std::vector<double> vt0(S, 0.0), vh(S, 0.0), vhI(S, 0.0), vhl(S, 0.0);
     std::vector<long long> vns(S, 0);
     for (int q = 0; q < nsg; q++) {
       int s = gp.systems[q];
       sidx[q] = s; vntt[q] = desc[s].ntt; vti[q] = desc[s].ti;
       vt0[q] = t_host[s]; vh[q] = hsig[s]; vhI[q] = desc[s].h; vns[q] = nsteps[s];
+      if (plain) vhl[q] = plain[s].hlast;
     }
+    if (plain) NBG_CUDA(cudaMemcpyAsync(hlast, vhl.data(), sizeof(double) * S, cudaMemcpyHostToDevice, st));
     NBG_CUDA(cudaMemcpyAsync(g.sysidx, sidx.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
     NBG_CUDA(cudaMemcpyAsync(g.ntt, vntt.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
     NBG_CUDA(cudaMemcpyAsync(g.ti, vti.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
@@ -559,8 +585,8 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
         if (c * K >= gmaxsteps[q]) continue;
         NBG_CUDA(cudaMemsetAsync(g.task_count, 0, sizeof(int), st));
         if ((rc = timed(0, [&] { return kOrbit[g.N](g, (int)c, st); }))) return rc;
-        if ((rc = timed(2, [&] { return kTransit[g.N](g, (int)c, st); }))) return rc;
-        ctx->last_launches += 2;
+        if (!g.notransit && (rc = timed(2, [&] { return kTransit[g.N](g, (int)c, st); }))) return rc;
+        ctx->last_launches += g.notransit ? 1 : 2;
         ctx->last_orbit_launches++;
         if (g.grad) {
           if ((rc = timed(3, [&] { return kOps[g.N](g, (int)c, st); }))) return rc;
@@ -607,9 +633,9 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
         NBG_CUDA(cudaEventRecord(ev_orb, sp));
         NBG_CUDA(cudaStreamWaitEvent(stt, ev_orb, 0));
         NBG_CUDA(cudaStreamWaitEvent(sw, ev_orb, 0));
-        if ((rc = timed_on(stt, 2, [&] { return kTransit[g.N](g, (int)c, stt); }))) return rc;
+        if (!g.notransit && (rc = timed_on(stt, 2, [&] { return kTransit[g.N](g, (int)c, stt); }))) return rc;
         NBG_CUDA(cudaEventRecord(ev_tr, stt));
-        ctx->last_launches += 2;
+        ctx->last_launches += g.notransit ? 1 : 2;
         ctx->last_orbit_launches++;
         if (g.grad) {
           if ((rc = timed_on(sw, 3, [&] { return kOps[g.N](g, (int)c, sw); }))) return rc;
@@ -647,15 +673,17 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
       ctx->last_launches++;
     }
   }
-  {
+  if (!plain) {
     dim3 grid(8, std::min(nsys, 65535), (nsys + 65534) / 65535);
     dtdelements_kernel<<<grid, 256, 0, st>>>(nsys, nullptr, d_off, d_dq0, d_jinit, d_dtdel, d_count, 0);
     ctx->last_launches++;
   }
-  // s.t = t0 + nsteps * h (Transits.jl:161 at the last step)
+  // s.t = t0 + nsteps * h (Transits.jl:161 at the last step); the plain
+  // drivers set it themselves (Integrator.jl:196, :228)
   {
     std::vector<double> tout(nsys);
-    for (int s = 0; s < nsys; s++) tout[s] = nsteps[s] > 0 ? t_host[s] + (double)nsteps[s] * hsig[s] : t_host[s];
+    for (int s = 0; s < nsys; s++)
+      tout[s] = plain ? plain[s].tout : (nsteps[s] > 0 ? t_host[s] + (double)nsteps[s] * hsig[s] : t_host[s]);
     NBG_CUDA(cudaMemcpyAsync(d_t, tout.data(), sizeof(double) * nsys, cudaMemcpyHostToDevice, st));
     NBG_CUDA(cudaStreamSynchronize(st));
   }
@@ -1215,6 +1243,130 @@ static int batch_host_device(nbg_context* ctx, int nsys, const nbg_system_desc* 
   NBG_CUDA(cudaMemcpyAsync(dtdelements, d_del, sizeof(double) * adq0, cudaMemcpyDeviceToHost, st));
   NBG_CUDA(cudaStreamSynchronize(st));
   return NBG_OK;
+}
+
+// Plain integration of nsys systems (host arrays, the packed layout of the
+// batched calls; no transit arrays).
+static int plain_host(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const PlainSpec* spec, double* t,
+                      double* x, double* v, const double* m, double* xerror, double* verror, double* jac_step,
+                      double* jac_error, double* dqdt, const uint8_t* pair) {
+  if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
+  if (nsys <= 0 || !desc) return set_error(NBG_EINVAL, "nsys = %d", nsys);
+  if (!t || !x || !v || !m || !xerror || !verror || !jac_step || !jac_error || !dqdt || !pair)
+    return set_error(NBG_EINVAL, "NULL array argument");
+  NBG_CUDA(cudaSetDevice(ctx->device));
+  long long ax = 0, am = 0, aJ = 0, adq = 0;
+  for (int s = 0; s < nsys; s++) {
+    const int n = desc[s].n, M = 7 * n;
+    if (n < NBG_MIN_BODIES || n > NBG_MAX_BODIES)
+      return set_error(NBG_EUNSUPPORTED, "system %d: n = %d outside %d..%d", s, n, NBG_MIN_BODIES, NBG_MAX_BODIES);
+    ax += 3 * n; am += n; aJ += (long long)M * M; adq += M;
+  }
+  cudaStream_t st = ctx->stream;
+  double *d_t, *d_x, *d_v, *d_m, *d_xe, *d_ve, *d_J, *d_E, *d_dq;
+  long long* d_cnt;
+  int rc;
+#define GETB(ptr, nm, cnt) if ((rc = ctx->get(nm, (size_t)(cnt), &ptr))) return rc
+  GETB(d_t, "p_t", nsys); GETB(d_x, "p_x", ax); GETB(d_v, "p_v", ax); GETB(d_m, "p_m", am);
+  GETB(d_xe, "p_xe", ax); GETB(d_ve, "p_ve", ax); GETB(d_J, "p_J", aJ); GETB(d_E, "p_E", aJ);
+  GETB(d_dq, "p_dq", adq); GETB(d_cnt, "p_cnt", am);
+#undef GETB
+  NBG_CUDA(cudaMemcpyAsync(d_x, x, sizeof(double) * ax, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_v, v, sizeof(double) * ax, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_m, m, sizeof(double) * am, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_xe, xerror, sizeof(double) * ax, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_ve, verror, sizeof(double) * ax, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_J, jac_step, sizeof(double) * aJ, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_E, jac_error, sizeof(double) * aJ, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemcpyAsync(d_dq, dqdt, sizeof(double) * adq, cudaMemcpyHostToDevice, st));
+  NBG_CUDA(cudaMemsetAsync(d_cnt, 0, sizeof(long long) * am, st));
+  rc = run_batch(ctx, nsys, desc, t, pair, d_t, d_x, d_v, d_m, d_xe, d_ve, d_J, d_E, d_dq, nullptr, nullptr, nullptr,
+                 nullptr, d_cnt, nullptr, spec);
+  if (rc) return rc;
+  NBG_CUDA(cudaMemcpyAsync(t, d_t, sizeof(double) * nsys, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(x, d_x, sizeof(double) * ax, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(v, d_v, sizeof(double) * ax, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(xerror, d_xe, sizeof(double) * ax, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(verror, d_ve, sizeof(double) * ax, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(jac_step, d_J, sizeof(double) * aJ, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(jac_error, d_E, sizeof(double) * aJ, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(dqdt, d_dq, sizeof(double) * adq, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaStreamSynchronize(st));
+  return NBG_OK;
+}
+
+// intr(s, time) (Integrator.jl:159-197): nsteps = |round((time - t0)/h)|
+// steps of h * check_step(t0, time), then one step of time - tmax when
+// tmax = t0 + h nsteps falls short of time; s.t = time.
+static PlainSpec spec_to_time(double t0, double h, double time) {
+  PlainSpec p;
+  long long n = (long long)std::nearbyint((time - t0) / h);
+  if (n < 0) n = -n;
+  const double hs = h * check_step(t0, time);
+  const double tmax = t0 + (hs * (double)n);
+  p.nsteps = n;
+  p.h = hs;
+  p.hlast = hs;
+  if (tmax != time) {
+    p.nsteps = n + 1;
+    p.hlast = time - tmax;
+  }
+  p.tout = time;
+  return p;
+}
+
+int nbg_integrate(nbg_context* ctx, int n, double h, double time, int grad, double* t, double* x, double* v,
+                  const double* m, double* xerror, double* verror, double* jac_step, double* jac_error, double* dqdt,
+                  const uint8_t* pair) {
+  if (!t) return set_error(NBG_EINVAL, "NULL array argument");
+  if (!(h != 0.0) || !std::isfinite(h) || !std::isfinite(time) || !std::isfinite(t[0]))
+    return set_error(NBG_EINVAL, "h = %g, time = %g, t = %g", h, time, t[0]);
+  nbg_system_desc d;
+  d.n = n; d.ti = 0; d.grad = grad ? 1 : 0; d.ntt = 1; d.h = h; d.tmax = time;
+  const PlainSpec p = spec_to_time(t[0], h, time);
+  return plain_host(ctx, 1, &d, &p, t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair);
+}
+
+int nbg_integrate_steps(nbg_context* ctx, int n, double h, int64_t nsteps, int grad, double* t, double* x,
+                        double* v, const double* m, double* xerror, double* verror, double* jac_step,
+                        double* jac_error, double* dqdt, const uint8_t* pair) {
+  if (!t) return set_error(NBG_EINVAL, "NULL array argument");
+  if (!(h != 0.0) || !std::isfinite(h) || !std::isfinite(t[0])) return set_error(NBG_EINVAL, "h = %g", h);
+  if (nsteps < -(1LL << 40) || nsteps > (1LL << 40)) return set_error(NBG_EINVAL, "nsteps = %lld", (long long)nsteps);
+  // intr(s, N) (Integrator.jl:210-233): a negative N steps backward; s.t
+  // advances by a compensated sum of the signed step
+  PlainSpec p;
+  const double hs = nsteps < 0 ? -h : h;
+  p.nsteps = nsteps < 0 ? -nsteps : nsteps;
+  p.h = hs;
+  p.hlast = hs;
+  double ts = t[0], e = 0.0;
+  for (long long q = 0; q < p.nsteps; q++) {
+    e = e + hs;
+    const double tn = ts + e;
+    e = (ts - tn) + e;
+    ts = tn;
+  }
+  p.tout = ts;
+  nbg_system_desc d;
+  d.n = n; d.ti = 0; d.grad = grad ? 1 : 0; d.ntt = 1; d.h = h; d.tmax = hs * (double)p.nsteps;
+  return plain_host(ctx, 1, &d, &p, t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair);
+}
+
+int nbg_batch_integrate(nbg_context* ctx, int nsys, const nbg_system_desc* desc, double* t, double* x, double* v,
+                        const double* m, double* xerror, double* verror, double* jac_step, double* jac_error,
+                        double* dqdt, const uint8_t* pair) {
+  if (nsys <= 0 || !desc || !t) return set_error(NBG_EINVAL, "nsys = %d", nsys);
+  std::vector<nbg_system_desc> d(desc, desc + nsys);
+  std::vector<PlainSpec> p(nsys);
+  for (int s = 0; s < nsys; s++) {
+    if (!(d[s].h != 0.0) || !std::isfinite(d[s].h) || !std::isfinite(d[s].tmax) || !std::isfinite(t[s]))
+      return set_error(NBG_EINVAL, "system %d: h = %g, time = %g", s, d[s].h, d[s].tmax);
+    d[s].ti = 0;
+    d[s].ntt = 1;
+    p[s] = spec_to_time(t[s], d[s].h, d[s].tmax);
+  }
+  return plain_host(ctx, nsys, d.data(), p.data(), t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair);
 }
 
 int nbg_integrate_transits(nbg_context* ctx, int n, int ti, double h, double tmax, int grad, double* t, double* x,

@@ -51,16 +51,18 @@ __global__ void __launch_bounds__(PROD_BS) orbit_chunk_kernel(GroupArgs g, int c
   for (int kk = 0; kk < g.K; kk++) {
     const long long istep = k0 + kk;
     if (istep >= nst) break;
+    const double hs = step_length(g, s, istep, nst, h);
     if (g.grad) {
       // x, v only; the operators are built from the captures by the operator
       // kernels.  The last step also computes dq/dt, the State's output.
       Rec cap{g.pcap + (size_t)kk * 2 * g.npk * PCAP * S + s, S};
       Rec xs{g.xsnap + (size_t)kk * snap_count(kick != 0) * 3 * N * S + s, S};
-      if (istep == nst - 1) ahl21_step<N, true, true>(st, w, h, kick, Rec{nullptr, 0}, cap, xs);
-      else ahl21_step<N, false, false>(st, w, h, kick, Rec{nullptr, 0}, cap, xs);
+      if (istep == nst - 1) ahl21_step<N, true, true>(st, w, hs, kick, Rec{nullptr, 0}, cap, xs);
+      else ahl21_step<N, false, false>(st, w, hs, kick, Rec{nullptr, 0}, cap, xs);
     } else {
-      ahl21_step<N, false, false>(st, w, h, kick, Rec{nullptr, 0}, Rec{nullptr, 0}, Rec{nullptr, 0});
+      ahl21_step<N, false, false>(st, w, hs, kick, Rec{nullptr, 0}, Rec{nullptr, 0}, Rec{nullptr, 0});
     }
+    if (g.notransit) continue;
     const double t = t0 + (double)(istep + 1) * h;
     // detect_transits! (timing.jl:3-28).  The search itself (findtransit!) is
     // queued: it runs from a copy of this state in transit_kernel, with full
@@ -234,9 +236,10 @@ __global__ void __launch_bounds__(OPS_BS) operator_phi_kernel(GroupArgs g, int c
   if (L >= (long long)g.K * S) return;
   const int s = (int)(L % S), kk = (int)(L / S);
   if (g.sysidx[s] < 0) return;
-  if (chunk_first_step(g, chunk, s) + kk >= g.nsteps[s]) return;
+  const long long istep = chunk_first_step(g, chunk, s) + kk;
+  if (istep >= g.nsteps[s]) return;
   const uint64_t kick = g.kick;
-  const double h = g.h[s];
+  const double h = step_length(g, s, istep, g.nsteps[s], g.h[s]);
   Rec xs{g.xsnap + (size_t)kk * snap_count(kick != 0) * 3 * N * S + s, S};
   Rec rec{g.steprec + (size_t)kk * g.R * S + s, S};
   Sys<N> st;
@@ -287,7 +290,8 @@ __global__ void __launch_bounds__(CONS_BS) jacobian_chunk_kernel(GroupArgs g, in
     const long long istep = k0 + kk;
     if (istep >= nst) break;
     Rec rec{g.steprec + (size_t)kk * g.R * S + s, S};
-    apply_step<N, CONS_BS>(J, E, c, h, kick, rec);
+    apply_step<N, CONS_BS>(J, E, c, step_length(g, s, istep, nst, h), kick, rec);
+    if (g.notransit) continue;
     for (int o = 0; o < N - 1; o++) {
       const int flag = g.tflag[(size_t)(kk * (N - 1) + o) * S + s];
       if (flag < 0) continue;

@@ -47,6 +47,10 @@ struct GroupArgs {
   // first chunk of each slot, in steps (null: every system starts at chunk 0);
   // the request server admits systems into running groups this way
   const long long* kbase;
+  // length of each system's last step (null: h); the plain integration
+  // drivers end on a fractional step (Integrator.jl:187-194)
+  const double* hlast;
+  int notransit;  // 1: no transit detection (the plain integration drivers)
   int *ntt, *ti, *sysidx;
   unsigned int* status;
   // packed outputs in the caller's layout, indexed by global system
@@ -71,6 +75,11 @@ struct GroupArgs {
   double* pcap;   // [K][2 npk][28][S]: Kepler-pair parameters
   double* xsnap;  // [K][snaps][3N][S]: positions at the correctors (and kicks)
 };
+
+// Length of step istep of the system in slot s (nst steps in all).
+__device__ __forceinline__ double step_length(const GroupArgs& g, int s, long long istep, long long nst, double h) {
+  return (g.hlast && istep == nst - 1) ? g.hlast[s] : h;
+}
 
 // Index of the first step of chunk `chunk` for the system in slot s.
 __device__ __forceinline__ long long chunk_first_step(const GroupArgs& g, int chunk, int s) {

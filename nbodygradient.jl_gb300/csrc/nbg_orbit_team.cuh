@@ -176,12 +176,13 @@ __global__ void __launch_bounds__(PROD_BS) orbit_team_kernel(GroupArgs g, int ch
       cap = Rec{g.pcap + (size_t)kk * 2 * g.npk * PCAP * S + s, S};
       xs = Rec{g.xsnap + (size_t)kk * snap_count(false) * 3 * N * S + s, S};
     }
-    team_step<N>(st, acc[tm], w, t, run && !last, h, cap, xs);
+    const double hs = run ? step_length(g, s, istep, nst, h) : h;
+    team_step<N>(st, acc[tm], w, t, run && !last, hs, cap, xs);
     // the last step also forms dq/dt: the one-lane step, on the team's first lane
-    if (last && t == 0) ahl21_step<N, true, true>(st, w, h, 0, Rec{nullptr, 0}, cap, xs);
+    if (last && t == 0) ahl21_step<N, true, true>(st, w, hs, 0, Rec{nullptr, 0}, cap, xs);
     __syncwarp();
     // detect_transits! (timing.jl:3-28); occultor o on lane o % L
-    if (run) {
+    if (run && !g.notransit) {
       const double tnow = t0 + (double)(istep + 1) * h;
       for (int o = t; o < N - 1; o += L) {
         const int ib = (o < ti) ? o : o + 1;

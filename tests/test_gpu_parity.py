@@ -230,3 +230,61 @@ def test_team_producer_is_bitwise_the_one_lane_producer(grad):
     assert sum(int(c) for c in out[0].arrays["count"]) > 0
     for k in ("x", "v", "xerror", "verror", "tt", "count", "jac_step", "jac_error", "dtdq0", "dtdelements", "dqdt"):
         assert np.array_equal(out[0].arrays[k], out[1].arrays[k]), k
+
+
+@pytest.mark.parametrize("n", [3, 5, 8])
+@pytest.mark.parametrize("grad", [True, False])
+def test_plain_integration_to_time(n, grad):
+    """intr(s, time) (Integrator.jl:159-197) with a fractional last step, forward and back."""
+    els, hs, _ = W.batch_uneven(2, seed=60 + n, nmin=n, nmax=n)
+    el, h = els[0], hs[0]
+    for time in (37.3 * h + 0.123 * h, -21.6 * h):
+        ic = nbg.ElementsIC(0.0, n, el)
+        s = nbg.State(ic)
+        so = O.OState(s.x.copy(order="F"), s.v.copy(order="F"), ic.m, jac_init=s.jac_init.copy(order="F"), t=0.0)
+        nbg.Integrator(nbg.ahl21, h, 0.0, 100.0)(s, float(time), grad=grad)
+        O.integrate_time(so, h, time, grad=grad)
+        assert s.t[0] == so.t[0] == time
+        P.check_state(s, so, check_jac=grad)
+
+
+def test_plain_integration_steps_and_default():
+    """intr(s, N) for N > 0 and N < 0 (Integrator.jl:210-233) and intr(s) (Integrator.jl:247)."""
+    el, h, _ = W.plain_3body(2)
+    ic = nbg.ElementsIC(0.0, 3, el)
+    for N in (57, -33):
+        s = nbg.State(ic)
+        so = O.OState(s.x.copy(order="F"), s.v.copy(order="F"), ic.m, jac_init=s.jac_init.copy(order="F"), t=0.0)
+        nbg.Integrator(nbg.ahl21, h, 0.0, 100.0)(s, N)
+        O.integrate_nsteps(so, h, N)
+        assert s.t[0] == so.t[0]
+        P.check_state(s, so)
+    s = nbg.State(ic)
+    s2 = nbg.State(ic)
+    intr = nbg.Integrator(nbg.ahl21, h, 0.0, 12.25)
+    intr(s)
+    intr(s2, 12.25)
+    for k in ("x", "v", "jac_step", "dqdt", "t"):
+        assert np.array_equal(getattr(s, k), getattr(s2, k)), k
+
+
+def test_plain_integration_batch_is_bitwise_single():
+    els, hs, tms = W.batch_uneven(10, seed=71, nmin=2, nmax=9)
+    states = [nbg.State(nbg.ElementsIC(0.0, el.shape[0], el)) for el in els]
+    times = [min(t, 41.7 * h) for t, h in zip(tms, hs)]
+    singles = [st.copy() for st in states]
+    for st, h, tm in zip(singles, hs, times):
+        nbg.Integrator(nbg.ahl21, h, 0.0, 1.0)(st, float(tm))
+    import ctypes
+    b = nbg.Batch([st.n for st in states], 0, hs, times, 1, True)
+    for q, st in enumerate(states):
+        b.set_system(q, st)
+    a = b.arrays
+    p = nbg._lib.ptr
+    nbg._lib.check(nbg._lib.load().nbg_batch_integrate(
+        nbg.default_context().handle, b.nsys, b.descriptors(), p(a["t"]), p(a["x"]), p(a["v"]), p(a["m"]),
+        p(a["xerror"]), p(a["verror"]), p(a["jac_step"]), p(a["jac_error"]), p(a["dqdt"]), p(a["pair"], nbg._lib._U8)))
+    for q, st in enumerate(singles):
+        for k in ("x", "v", "jac_step", "dqdt"):
+            assert np.array_equal(b.view(k, q), np.asarray(getattr(st, k)).ravel(order="F")), (q, k)
+        assert b.view("t", q)[0] == st.t[0] == times[q]
