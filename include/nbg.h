@@ -96,6 +96,25 @@ int nbg_integrate_transits(nbg_context* ctx, int n, int ti, double h, double tma
                            int64_t* count);
 
 /*
+ * (intr::Integrator)(s::State{Float64}, ttbv::TransitParameters{Float64}; grad)
+ * Replaces src/transits/Transits.jl:140-180 with a TransitParameters output
+ * (Transits.jl:68-110) and the TransitParameters branch of findtransit!
+ * (src/transits/timing.jl:82-98, dtbvdq! rows 1-3 at :155-193,
+ * calc_dtdelements! at :126-138).  Same State arguments as
+ * nbg_integrate_transits; the outputs carry a leading row index r = t,
+ * v_sky, b_sky^2:
+ *   ttbv                   : 3 x n x ntt          (A[r + 3(j + n c)])
+ *   dtbvdq0, dtbvdelements : 3 x n x ntt x 7 x n  (A[r + 3(j + n(c + ntt(k + 7p)))])
+ * Without grad, v_sky and b_sky^2 are those of the last Newton iterate's
+ * state, as in the reference.
+ */
+int nbg_integrate_transit_parameters(nbg_context* ctx, int n, int ti, double h, double tmax, int grad, double* t,
+                                     double* x, double* v, const double* m, double* xerror, double* verror,
+                                     double* jac_step, double* jac_error, double* dqdt, const uint8_t* pair,
+                                     const double* jac_init, int64_t ntt, double* ttbv, double* dtbvdq0,
+                                     double* dtbvdelements, int64_t* count);
+
+/*
  * (intr::Integrator)(s::State{Float64}, time::Float64; grad)
  * Replaces src/integrator/Integrator.jl:159-197 with intr.scheme === ahl21!:
  * nsteps = |round((time - s.t)/h)| steps of h * check_step(s.t, time), then,
@@ -141,6 +160,18 @@ int nbg_batch_integrate_transits(nbg_context* ctx, int nsys, const nbg_system_de
                                  double* v, const double* m, double* xerror, double* verror, double* jac_step,
                                  double* jac_error, double* dqdt, const uint8_t* pair, const double* jac_init,
                                  double* tt, double* dtdq0, double* dtdelements, int64_t* count, uint32_t* status);
+
+/*
+ * nbg_integrate_transit_parameters for nsys systems in one plan (arguments
+ * as nbg_batch_integrate_transits; ttbv / dtbvdq0 / dtbvdelements packed
+ * with 3 n ntt and 3 n ntt 7 n doubles per system).  No reference
+ * counterpart (the reference loops in Julia).
+ */
+int nbg_batch_integrate_transit_parameters(nbg_context* ctx, int nsys, const nbg_system_desc* desc, double* t,
+                                           double* x, double* v, const double* m, double* xerror, double* verror,
+                                           double* jac_step, double* jac_error, double* dqdt, const uint8_t* pair,
+                                           const double* jac_init, double* ttbv, double* dtbvdq0,
+                                           double* dtbvdelements, int64_t* count, uint32_t* status);
 
 /*
  * nbg_integrate for nsys systems in one plan: desc[s].tmax is system s's

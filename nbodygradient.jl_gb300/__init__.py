@@ -24,7 +24,8 @@ from . import _lib, build, workloads
 from ._lib import Context, NbgError, SystemDesc, default_context, device_info
 from .ics import CartesianIC, Elements, ElementsIC, hierarchy_nested, init_nbody, kepler_init
 
-__all__ = ["Elements", "ElementsIC", "CartesianIC", "State", "TransitTiming", "Integrator", "ahl21", "set_state",
+__all__ = ["Elements", "ElementsIC", "CartesianIC", "State", "TransitTiming", "TransitParameters", "Integrator",
+           "ahl21", "set_state",
            "Context", "NbgError", "default_context", "device_info", "integrate_transits_batch", "Batch", "Server",
            "hierarchy_nested", "init_nbody", "kepler_init"]
 
@@ -107,6 +108,32 @@ class TransitTiming:
         self.count[...] = 0
 
 
+class TransitParameters:
+    """Transit times, sky velocities, impact parameters and derivatives
+    (src/transits/Transits.jl:68-110).  ttbv[0] = t, ttbv[1] = v_sky,
+    ttbv[2] = b_sky^2 (row index first, as the reference's 3 x n x ntt)."""
+
+    def __init__(self, tmax, ic, ti=1, ntt=None):
+        n = ic.nbody
+        if not (1 <= ti <= n):
+            raise ValueError("ti must be in 1..%d" % n)
+        ntt_ref = _ntt(tmax, ic.elements[:, 1])
+        if ntt is not None and ntt < ntt_ref:
+            raise ValueError("ntt = %d is below the reference's %d" % (ntt, ntt_ref))
+        ntt = ntt_ref if ntt is None else int(ntt)
+        self.n, self.ntt, self.ti = n, ntt, ti
+        self.ttbv = np.zeros((3, n, ntt), order="F")
+        self.dtbvdq0 = np.zeros((3, n, ntt, 7, n), order="F")
+        self.dtbvdelements = np.zeros((3, n, ntt, 7, n), order="F")
+        self.count = np.zeros(n, dtype=np.int64)
+        self.occs = [i for i in range(1, n + 1) if i != ti]
+
+    def zero_out(self):
+        for a in (self.ttbv, self.dtbvdq0, self.dtbvdelements):
+            a[...] = 0.0
+        self.count[...] = 0
+
+
 class Integrator:
     """Integrator(scheme, h, t0, tmax) (src/integrator/Integrator.jl:17-31).
 
@@ -149,8 +176,15 @@ class Integrator:
             else:
                 _lib.check(L.nbg_integrate(ctx.handle, s.n, self.h, float(tt), int(bool(grad)), *args))
             return None
+        if isinstance(tt, TransitParameters):
+            _lib.check(L.nbg_integrate_transit_parameters(
+                ctx.handle, s.n, tt.ti - 1, self.h, self.tmax, int(bool(grad)), p(s.t), p(s.x), p(s.v), p(s.m),
+                p(s.xerror), p(s.verror), p(s.jac_step), p(s.jac_error), p(s.dqdt), p(s.pair, _lib._U8),
+                p(s.jac_init), tt.ntt, p(tt.ttbv), p(tt.dtbvdq0), p(tt.dtbvdelements), p(tt.count, _lib._I64)))
+            return None
         if not isinstance(tt, TransitTiming):
-            raise NbgError(_lib.NBG_EUNSUPPORTED, "intr(s, tt) takes a TransitTiming, a time or a step count")
+            raise NbgError(_lib.NBG_EUNSUPPORTED,
+                           "intr(s, tt) takes a TransitTiming, a TransitParameters, a time or a step count")
         _lib.check(L.nbg_integrate_transits(
             ctx.handle, s.n, tt.ti - 1, self.h, self.tmax, int(bool(grad)), p(s.t), p(s.x), p(s.v), p(s.m),
             p(s.xerror), p(s.verror), p(s.jac_step), p(s.jac_error), p(s.dqdt), p(s.pair, _lib._U8), p(s.jac_init),

@@ -34,6 +34,7 @@ EXPORTS = (
     "nbg_set_profiling", "nbg_last_kernel_stats", "nbg_set_orbit_lanes", "nbg_set_orbit_team",
     "nbg_batch_integrate_transits_noalloc",
     "nbg_integrate", "nbg_integrate_steps", "nbg_batch_integrate",
+    "nbg_integrate_transit_parameters", "nbg_batch_integrate_transit_parameters",
     "nbg_server_start", "nbg_server_enqueue", "nbg_server_wait_any", "nbg_server_poll", "nbg_server_stats",
     "nbg_server_stop",
 )
@@ -115,6 +116,8 @@ def load(build_if_missing=True):
     batch_args = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc), _D, _D, _D, _D, _D, _D, _D, _D, _D, _U8, _D, _D, _D,
                   _D, _I64, _U32]
     L.nbg_batch_integrate_transits.argtypes = batch_args
+    L.nbg_batch_integrate_transit_parameters.argtypes = batch_args
+    L.nbg_integrate_transit_parameters.argtypes = L.nbg_integrate_transits.argtypes
     L.nbg_batch_integrate_transits_device.argtypes = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc)] + [_VP] * 16
     L.nbg_batch_integrate_transits_noalloc.argtypes = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc)] + [_VP] * 16
     L.nbg_set_tuning.argtypes = [_VP, ctypes.c_int, ctypes.c_int]

@@ -122,19 +122,22 @@ __global__ void dtdelements_kernel(int nsys, const int* list, const SysOff* off,
   const int gs = list ? list[y] : y;
   const SysOff o = off[gs];
   if (!o.grad) return;
-  const int n = o.n, ntt = o.ntt, M = 7 * n;
-  const long long tot = (long long)n * ntt * 7 * n;
+  const int n = o.n, ntt = o.ntt, M = 7 * n, nr = o.nr > 1 ? o.nr : 1;
+  const long long tot = (long long)nr * n * ntt * 7 * n;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
-    const int j = (int)(e % n);
-    const long long c = (e / n) % ntt;
-    const int l = (int)((e / ((long long)n * ntt)) % 7);
-    const int k = (int)(e / ((long long)n * ntt * 7));
+    // e = r + nr (j + n (c + ntt (l + 7 k)))
+    const int r = (int)(e % nr);
+    const long long e1 = e / nr;
+    const int j = (int)(e1 % n);
+    const long long c = (e1 / n) % ntt;
+    const int l = (int)((e1 / ((long long)n * ntt)) % 7);
+    const int k = (int)(e1 / ((long long)n * ntt * 7));
     const long long cnt = count[o.cnt + j];
     if (c >= cnt || c >= ntt) continue;
     double acc = 0.0;
     for (int p = 0; p < n; p++)
       for (int q = 0; q < 7; q++)
-        acc = acc + dtdq0[o.dq + j + (long long)n * (c + (long long)ntt * (q + 7LL * p))] *
+        acc = acc + dtdq0[o.dq + r + nr * (j + (long long)n * (c + (long long)ntt * (q + 7LL * p)))] *
                         jac_init[o.J + (7 * p + q) + (long long)M * (7 * k + l)];
     dtdel[o.dq + (after_dtdq0 ? tot : 0) + e] = acc;
   }
@@ -351,7 +354,8 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
               const uint8_t* pair_host, double* d_t, double* d_x, double* d_v, const double* d_m, double* d_xe,
               double* d_ve, double* d_J, double* d_E, double* d_dqdt, const double* d_jinit, double* d_tt,
               double* d_dq0, double* d_dtdel, long long* d_count, uint32_t* status_host,
-              const PlainSpec* plain = nullptr) {
+              const PlainSpec* plain = nullptr, int tbv = 0) {
+  const int nr = tbv ? 3 : 1;  // rows per transit of the outputs
   cudaStream_t st = ctx->stream;
   ctx->last_launches = 0;
   ctx->last_orbit_ms = ctx->last_jac_ms = ctx->last_transit_ms = ctx->last_ops_ms = 0;
@@ -373,9 +377,9 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     const int n = d.n, M = 7 * n;
     SysOff& o = off[s];
     o.x = ax; o.m = am; o.J = aJ; o.dqdt = adq; o.pair = ap; o.tt = att; o.dq = adq0; o.cnt = acn;
-    o.n = n; o.ntt = d.ntt; o.grad = d.grad ? 1 : 0; o.pad = 0;
+    o.n = n; o.ntt = d.ntt; o.grad = d.grad ? 1 : 0; o.nr = nr;
     ax += 3 * n; am += n; aJ += (long long)M * M; adq += M; ap += (long long)n * n;
-    att += (long long)n * d.ntt; adq0 += (long long)n * d.ntt * 7 * n; acn += n;
+    att += (long long)nr * n * d.ntt; adq0 += (long long)nr * n * d.ntt * 7 * n; acn += n;
     if (plain) {
       nsteps[s] = plain[s].nsteps;
       hsig[s] = plain[s].h;
@@ -437,7 +441,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     const int S = ((nsg + 31) / 32) * 32;
     GroupArgs g;
     memset(&g, 0, sizeof(g));
-    g.N = N; g.S = S; g.nsys = nsg; g.grad = gp.grad; g.K = K; g.kick = gp.kick;
+    g.N = N; g.S = S; g.nsys = nsg; g.grad = gp.grad; g.K = K; g.kick = gp.kick; g.tbv = tbv;
     // Orbit producer lanes per warp.  A warp's FP64 instruction occupies its
     // SM sub-partition's FP64 pipe for the same time at any lane count, and
     // one producer warp per sub-partition runs its chain at the same speed
@@ -477,7 +481,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     // Per-chunk buffers (the transit queue, the captures and the records) are
     // double-buffered in overlap mode: chunk c uses half c % 2.
     const size_t nf = (size_t)g.task_cap * (12 * N + 2), ni = (size_t)g.task_cap * 3;
-    const size_t nrec = (size_t)K * g.R * S, ntrec = (size_t)K * (N - 1) * (7 * N + 1) * S;
+    const size_t nrec = (size_t)K * g.R * S, ntrec = (size_t)K * (N - 1) * trec_size(N, tbv) * S;
     const size_t nflag = (size_t)K * (N - 1) * S, ncap = (size_t)K * 2 * npk * PCAP * S + 1;
     const size_t nsnap = (size_t)K * snap_count(gp.kick != 0) * 3 * N * S;
     const int nb = ctx->overlap ? 2 : 1;
@@ -774,7 +778,7 @@ void noalloc_layout(NoallocPlan& P, ScratchArena& a, int nsys, int K, int tcap, 
     a.take(&g.task_f, (size_t)g.task_cap * (12 * N + 2)); a.take(&g.task_i, (size_t)g.task_cap * 3);
     a.take(&g.task_count, 1);
     if (g.grad) {
-      a.take(&g.steprec, (size_t)K * g.R * S); a.take(&g.trec, (size_t)K * (N - 1) * (7 * N + 1) * S);
+      a.take(&g.steprec, (size_t)K * g.R * S); a.take(&g.trec, (size_t)K * (N - 1) * trec_size(N, 0) * S);
       a.take(&g.tflag, (size_t)K * (N - 1) * S); a.take(&g.tscratch, (size_t)g.R * g.tgrid);
       a.take(&g.pcap, (size_t)K * 2 * g.npk * PCAP * S + 1);
       a.take(&g.xsnap, (size_t)K * snap_count(g.kick != 0) * 3 * N * S);
@@ -805,7 +809,7 @@ int run_batch_noalloc(nbg_context* ctx, NoallocPlan& P, int nsys, const nbg_syst
     const int n = d.n, M = 7 * n;
     SysOff& o = P.off[s];
     o.x = ax; o.m = am; o.J = aJ; o.dqdt = adq; o.pair = ap; o.tt = att; o.dq = adq0; o.cnt = acn;
-    o.n = n; o.ntt = d.ntt; o.grad = d.grad ? 1 : 0; o.pad = 0;
+    o.n = n; o.ntt = d.ntt; o.grad = d.grad ? 1 : 0; o.nr = 0;
     P.offtt[s] = att;
     P.offdq[s] = adq0;
     ax += 3 * n; am += n; aJ += (long long)M * M; adq += M; ap += (long long)n * n;
@@ -1180,7 +1184,9 @@ int nbg_fp64_peak(nbg_context* ctx, double* tflops) {
 static int batch_host_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc, double* t, double* x,
                              double* v, const double* m, double* xerror, double* verror, double* jac_step,
                              double* jac_error, double* dqdt, const uint8_t* pair, const double* jac_init, double* tt,
-                             double* dtdq0, double* dtdelements, int64_t* count, uint32_t* status, bool copy_outputs_in) {
+                             double* dtdq0, double* dtdelements, int64_t* count, uint32_t* status, bool copy_outputs_in,
+                             int tbv = 0) {
+  const int nr = tbv ? 3 : 1;
   if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
   if (nsys <= 0 || !desc) return set_error(NBG_EINVAL, "nsys = %d", nsys);
   NBG_CUDA(cudaSetDevice(ctx->device));
@@ -1191,7 +1197,7 @@ static int batch_host_device(nbg_context* ctx, int nsys, const nbg_system_desc* 
       return set_error(NBG_EUNSUPPORTED, "system %d: n = %d outside %d..%d", s, n, NBG_MIN_BODIES, NBG_MAX_BODIES);
     if (desc[s].ntt < 1) return set_error(NBG_EINVAL, "system %d: ntt = %d", s, desc[s].ntt);
     ax += 3 * n; am += n; aJ += (long long)M * M; adq += M; ap += (long long)n * n;
-    att += (long long)n * desc[s].ntt; adq0 += (long long)n * desc[s].ntt * 7 * n;
+    att += (long long)nr * n * desc[s].ntt; adq0 += (long long)nr * n * desc[s].ntt * 7 * n;
   }
   if (!copy_outputs_in)
     for (long long q = 0; q < am; q++)
@@ -1227,7 +1233,7 @@ static int batch_host_device(nbg_context* ctx, int nsys, const nbg_system_desc* 
     NBG_CUDA(cudaMemsetAsync(d_del, 0, sizeof(double) * adq0, st));
   }
   rc = run_batch(ctx, nsys, desc, t, pair, d_t, d_x, d_v, d_m, d_xe, d_ve, d_J, d_E, d_dq, d_ji, d_tt, d_dq0, d_del,
-                 d_cnt, status);
+                 d_cnt, status, nullptr, tbv);
   if (rc) return rc;
   NBG_CUDA(cudaMemcpyAsync(t, d_t, sizeof(double) * nsys, cudaMemcpyDeviceToHost, st));
   NBG_CUDA(cudaMemcpyAsync(x, d_x, sizeof(double) * ax, cudaMemcpyDeviceToHost, st));
@@ -1384,6 +1390,33 @@ int nbg_integrate_transits(nbg_context* ctx, int n, int ti, double h, double tma
   if (ti < 0 || ti >= n) return set_error(NBG_EINVAL, "ti = %d not in 0..%d", ti, n - 1);
   return batch_host_device(ctx, 1, &d, t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair, jac_init, tt,
                            dtdq0, dtdelements, count, nullptr, true);
+}
+
+int nbg_integrate_transit_parameters(nbg_context* ctx, int n, int ti, double h, double tmax, int grad, double* t,
+                                     double* x, double* v, const double* m, double* xerror, double* verror,
+                                     double* jac_step, double* jac_error, double* dqdt, const uint8_t* pair,
+                                     const double* jac_init, int64_t ntt, double* ttbv, double* dtbvdq0,
+                                     double* dtbvdelements, int64_t* count) {
+  if (!t || !x || !v || !m || !xerror || !verror || !jac_step || !jac_error || !dqdt || !pair || !jac_init ||
+      !ttbv || !dtbvdq0 || !dtbvdelements || !count)
+    return set_error(NBG_EINVAL, "NULL array argument");
+  if (ntt < 1 || ntt > (1LL << 30)) return set_error(NBG_EINVAL, "ntt = %lld", (long long)ntt);
+  if (n < NBG_MIN_BODIES || n > NBG_MAX_BODIES)
+    return set_error(NBG_EUNSUPPORTED, "n = %d outside %d..%d", n, NBG_MIN_BODIES, NBG_MAX_BODIES);
+  if (ti < 0 || ti >= n) return set_error(NBG_EINVAL, "ti = %d not in 0..%d", ti, n - 1);
+  nbg_system_desc d;
+  d.n = n; d.ti = ti; d.grad = grad ? 1 : 0; d.ntt = (int32_t)ntt; d.h = h; d.tmax = tmax;
+  return batch_host_device(ctx, 1, &d, t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair, jac_init, ttbv,
+                           dtbvdq0, dtbvdelements, count, nullptr, true, 1);
+}
+
+int nbg_batch_integrate_transit_parameters(nbg_context* ctx, int nsys, const nbg_system_desc* desc, double* t,
+                                           double* x, double* v, const double* m, double* xerror, double* verror,
+                                           double* jac_step, double* jac_error, double* dqdt, const uint8_t* pair,
+                                           const double* jac_init, double* ttbv, double* dtbvdq0,
+                                           double* dtbvdelements, int64_t* count, uint32_t* status) {
+  return batch_host_device(ctx, nsys, desc, t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair, jac_init,
+                           ttbv, dtbvdq0, dtbvdelements, count, status, false, 1);
 }
 
 int nbg_batch_integrate_transits(nbg_context* ctx, int nsys, const nbg_system_desc* desc, double* t, double* x,

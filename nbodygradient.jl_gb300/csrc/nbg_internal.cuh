@@ -12,10 +12,12 @@ namespace nbg {
 
 // Offsets of one system into packed arrays in the caller's layout (element
 // counts, not bytes).  x/v/xerror/verror share `x`; jac_step/jac_error/
-// jac_init share `J`; dtdq0/dtdelements share `dq`.
+// jac_init share `J`; dtdq0/dtdelements share `dq`.  nr: rows per transit
+// of the outputs (1: TransitTiming; 3: TransitParameters' t, v_sky,
+// b_sky^2; 0 counts as 1).
 struct SysOff {
   long long x, m, J, dqdt, pair, tt, dq, cnt;
-  int n, ntt, grad, pad;
+  int n, ntt, grad, nr;
 };
 
 // Records the calling thread's error message and returns `code`.

@@ -168,6 +168,16 @@ __global__ void __launch_bounds__(TRANSIT_BS) transit_kernel(GroupArgs g, int ch
       if (iter >= 20 || dt0 == tt1 || dt0 == tt2) break;
     }
     if (iter >= 20) atomicOr(g.status + s, NBG_STATUS_NEWTON_ITMAX);
+    const int nr = g.tbv ? 3 : 1;
+    double* ttout = g.tt + g.off_tt[g.sysidx[s]] + (long long)nr * (ib + (long long)N * c);
+    if (g.tbv && !g.grad) {
+      // TransitParameters without gradient (timing.jl:96-97): v_sky and
+      // b_sky^2 of the last Newton iteration's state
+      const double dvx = wk.v[3 * ib] - wk.v[3 * ti], dvy = wk.v[3 * ib + 1] - wk.v[3 * ti + 1];
+      const double dx = wk.x[3 * ib] - wk.x[3 * ti], dy = wk.x[3 * ib + 1] - wk.x[3 * ti + 1];
+      ttout[1] = sqrt(dvx * dvx + dvy * dvy);
+      ttout[2] = dx * dx + dy * dy;
+    }
     if (g.grad) {
       wk = st;
       Rec rec{g.tscratch + tid, G};
@@ -186,12 +196,44 @@ __global__ void __launch_bounds__(TRANSIT_BS) transit_kernel(GroupArgs g, int ch
       u[7 * ti + 4] = -dy;
       adjoint_step<N>(u, dt0, kick, rec);
       const double gd = gdot(wk, ti, ib);
-      double* tr = g.trec + ((size_t)slot * (7 * N + 1)) * S + s;
+      double* tr = g.trec + ((size_t)slot * trec_size(N, g.tbv)) * S + s;
       for (int q = 0; q < 7 * N; q++) tr[(size_t)q * S] = u[q];
-      tr[(size_t)(7 * N) * S] = gd;
+      if (g.tbv) {
+        // dtbvdq! rows 2 and 3 (timing.jl:173-191): v_sky and b_sky^2 of the
+        // converged state, dv_sky/dt, and the adjoint rows of their
+        // numerators (d v_sky: the sky velocity difference on the velocity
+        // rows; d b_sky^2 / 2: the sky position difference on the position rows)
+        const double vsky = sqrt(dvx * dvx + dvy * dvy);
+        const double bsky2 = dx * dx + dy * dy;
+        const double* q = wk.dqdt;
+        const double dvdt = (dvx * (q[7 * ib + 3] - q[7 * ti + 3]) + dvy * (q[7 * ib + 4] - q[7 * ti + 4])) / vsky;
+        for (int r = 0; r < 2; r++) {
+          for (int e = 0; e < 7 * N; e++) u[e] = 0.0;
+          if (r == 0) {
+            u[7 * ib + 3] = dvx;
+            u[7 * ti + 3] = -dvx;
+            u[7 * ib + 4] = dvy;
+            u[7 * ti + 4] = -dvy;
+          } else {
+            u[7 * ib + 0] = dx;
+            u[7 * ti + 0] = -dx;
+            u[7 * ib + 1] = dy;
+            u[7 * ti + 1] = -dy;
+          }
+          adjoint_step<N>(u, dt0, kick, rec);
+          for (int e = 0; e < 7 * N; e++) tr[(size_t)(7 * N * (r + 1) + e) * S] = u[e];
+        }
+        tr[(size_t)(21 * N) * S] = gd;
+        tr[(size_t)(21 * N + 1) * S] = vsky;
+        tr[(size_t)(21 * N + 2) * S] = dvdt;
+        ttout[1] = vsky;
+        ttout[2] = bsky2;
+      } else {
+        tr[(size_t)(7 * N) * S] = gd;
+      }
       g.tflag[(size_t)slot * S + s] = c;
     }
-    g.tt[g.off_tt[g.sysidx[s]] + ib + (long long)N * c] = t + dt0;
+    ttout[0] = t + dt0;
   }
 }
 
@@ -295,18 +337,40 @@ __global__ void __launch_bounds__(CONS_BS) jacobian_chunk_kernel(GroupArgs g, in
     for (int o = 0; o < N - 1; o++) {
       const int flag = g.tflag[(size_t)(kk * (N - 1) + o) * S + s];
       if (flag < 0) continue;
-      const double* tr = g.trec + ((size_t)(kk * (N - 1) + o) * (7 * N + 1)) * S + s;
-      double acc = 0.0;
-      for (int b = 0; b < N; b++)
-        for (int r = 0; r < 6; r++) {
-          const double ur = tr[(size_t)(7 * b + r) * S];
-          acc = fma(ur, J[(6 * b + r) * CONS_BS], acc);
-          acc = fma(ur, E[(6 * b + r) * CONS_BS], acc);
-        }
-      if (ck == 6) acc = acc + tr[(size_t)c * S];  // unit mass row of this column
-      const double gd = tr[(size_t)(7 * N) * S];
+      const double* tr = g.trec + ((size_t)(kk * (N - 1) + o) * trec_size(N, g.tbv)) * S + s;
       const int ib = (o < ti) ? o : o + 1;
-      g.dtdq0[g.off_dq[gsys] + ib + (long long)N * (flag + (long long)ntt * (ck + 7LL * cb))] = -acc / gd;
+      if (!g.tbv) {
+        double acc = 0.0;
+        for (int b = 0; b < N; b++)
+          for (int r = 0; r < 6; r++) {
+            const double ur = tr[(size_t)(7 * b + r) * S];
+            acc = fma(ur, J[(6 * b + r) * CONS_BS], acc);
+            acc = fma(ur, E[(6 * b + r) * CONS_BS], acc);
+          }
+        if (ck == 6) acc = acc + tr[(size_t)c * S];  // unit mass row of this column
+        const double gd = tr[(size_t)(7 * N) * S];
+        g.dtdq0[g.off_dq[gsys] + ib + (long long)N * (flag + (long long)ntt * (ck + 7LL * cb))] = -acc / gd;
+      } else {
+        double acc[3] = {0.0, 0.0, 0.0};
+        for (int b = 0; b < N; b++)
+          for (int r = 0; r < 6; r++) {
+            const double jv = J[(6 * b + r) * CONS_BS], ev = E[(6 * b + r) * CONS_BS];
+            for (int w = 0; w < 3; w++) {
+              const double ur = tr[(size_t)(7 * N * w + 7 * b + r) * S];
+              acc[w] = fma(ur, jv, acc[w]);
+              acc[w] = fma(ur, ev, acc[w]);
+            }
+          }
+        if (ck == 6)
+          for (int w = 0; w < 3; w++) acc[w] = acc[w] + tr[(size_t)(7 * N * w + c) * S];
+        const double gd = tr[(size_t)(21 * N) * S], vsky = tr[(size_t)(21 * N + 1) * S];
+        const double dvdt = tr[(size_t)(21 * N + 2) * S];
+        const double d1 = -acc[0] / gd;
+        double* out = g.dtdq0 + g.off_dq[gsys] + 3 * (ib + (long long)N * (flag + (long long)ntt * (ck + 7LL * cb)));
+        out[0] = d1;
+        out[1] = acc[1] / vsky + dvdt * d1;
+        out[2] = 2.0 * acc[2];
+      }
     }
   }
   double* Jw = g.Jint + (size_t)s * R6 * M + c;

@@ -26,6 +26,11 @@ constexpr int CONS_BS = 128;    // Jacobian consumer: four warps per block
 constexpr int TRANSIT_BS = 32;  // transit searches: one warp per block
 constexpr int OPS_BS = 128;     // operator kernels
 
+// Doubles per transit of the adjoint record: the row u^T = w^T S(dt0) of
+// the transit time and gdot (7N + 1); TransitParameters add the rows of
+// v_sky and b_sky^2, v_sky and d v_sky / dt (21N + 3).
+__host__ __device__ inline int trec_size(int N, int tbv) { return tbv ? 21 * N + 3 : 7 * N + 1; }
+
 // Captured Kepler-pair parameters (producer -> operator kernel): x0[3], v0[3]
 // and the 22 values jac_delxv_gamma! returns (ahl21.jl:888-889).
 constexpr int PCAP = 28;
@@ -51,6 +56,7 @@ struct GroupArgs {
   // drivers end on a fractional step (Integrator.jl:187-194)
   const double* hlast;
   int notransit;  // 1: no transit detection (the plain integration drivers)
+  int tbv;        // 1: TransitParameters outputs (t, v_sky, b_sky^2 per transit)
   int *ntt, *ti, *sysidx;
   unsigned int* status;
   // packed outputs in the caller's layout, indexed by global system

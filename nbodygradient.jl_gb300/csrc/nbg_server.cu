@@ -314,7 +314,7 @@ int create_group(nbg_server* srv, int N, int grad, unsigned long long kick, Grou
   want(&g.task_f, (size_t)g.task_cap * (12 * N + 2)); want(&g.task_i, (size_t)g.task_cap * 3);
   want(&g.task_count, 1);
   if (grad) {
-    want(&g.steprec, (size_t)K * g.R * S); want(&g.trec, (size_t)K * (N - 1) * (7 * N + 1) * S);
+    want(&g.steprec, (size_t)K * g.R * S); want(&g.trec, (size_t)K * (N - 1) * trec_size(N, 0) * S);
     want(&g.tflag, (size_t)K * (N - 1) * S); want(&g.tscratch, (size_t)g.R * g.tgrid);
     want(&g.pcap, (size_t)K * 2 * npk * PCAP * S + 1);
     want(&g.xsnap, (size_t)K * snap_count(kick != 0) * 3 * N * S);
@@ -482,7 +482,7 @@ int service_group(nbg_server* srv, int gi) {
       a.off.pair = 0;
       a.off.tt = (long long)r->heap_off;
       a.off.dq = (long long)r->heap_off + (long long)N * r->d.ntt;
-      a.off.n = N; a.off.ntt = r->d.ntt; a.off.grad = G->grad; a.off.pad = 0;
+      a.off.n = N; a.off.ntt = r->d.ntt; a.off.grad = G->grad; a.off.nr = 1;
       a.kbase = c * K;
       a.nsteps = r->nsteps;
       a.t0 = r->t0; a.h = r->hsig; a.hI = r->d.h;

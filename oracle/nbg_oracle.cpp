@@ -67,6 +67,39 @@ template <class T> static quad absmax(const std::vector<T>& a) {
 
 }  // namespace
 
+// R: the arithmetic type (double for parity; quad for the rounding-error
+// reference the parity tests use to size their tolerances).
+template <class R>
+static int integrate_transits_nr(int nr, int n, int ti, double h, double tmax, int grad, double* t, double* x,
+                                 double* v, const double* m, double* xerr, double* verr, double* jac_step,
+                                 double* jac_err, double* dqdt, const uint8_t* pair, const double* jac_init, int ntt,
+                                 double* tt, double* dtdq0, double* dtdelements, int64_t* count) {
+  if (n < 2 || ti < 0 || ti >= n || ntt < 1) return -1;
+  State<R> s;
+  load_state(s, n, x, v, m, xerr, verr, jac_step, jac_err, dqdt, pair, jac_init);
+  s.t = R(*t);
+  TransitTiming<R> T;
+  T.alloc(n, ntt, ti, nr);
+  size_t n4 = (size_t)nr * n * ntt * 7 * n;
+  for (size_t q = 0; q < (size_t)nr * n * ntt; q++) T.tt[q] = R(tt[q]);
+  for (size_t q = 0; q < n4; q++) {
+    T.dtdq0[q] = R(dtdq0[q]);
+    T.dtdelements[q] = R(dtdelements[q]);
+  }
+  for (int q = 0; q < n; q++) T.count[q] = count[q];
+  T.s_prior.alloc(n);
+  intr_transits(s, T, R(h), R(tmax), grad != 0);
+  store_state(s, x, v, xerr, verr, jac_step, jac_err, dqdt);
+  *t = (double)s.t;
+  for (size_t q = 0; q < T.tt.size(); q++) tt[q] = (double)T.tt[q];
+  for (size_t q = 0; q < n4; q++) {
+    dtdq0[q] = (double)T.dtdq0[q];
+    dtdelements[q] = (double)T.dtdelements[q];
+  }
+  for (int q = 0; q < n; q++) count[q] = T.count[q];
+  return 0;
+}
+
 extern "C" {
 
 int oracle_version(void) { return 1; }
@@ -90,26 +123,31 @@ int oracle_integrate_transits(int n, int ti, double h, double tmax, int grad, do
                               const double* m, double* xerr, double* verr, double* jac_step, double* jac_err,
                               double* dqdt, const uint8_t* pair, const double* jac_init, int ntt, double* tt,
                               double* dtdq0, double* dtdelements, int64_t* count) {
-  if (n < 2 || ti < 0 || ti >= n || ntt < 1) return -1;
-  State<double> s;
-  load_state(s, n, x, v, m, xerr, verr, jac_step, jac_err, dqdt, pair, jac_init);
-  s.t = *t;
-  TransitTiming<double> T;
-  T.alloc(n, ntt, ti);
-  size_t n4 = (size_t)n * ntt * 7 * n;
-  std::copy(tt, tt + (size_t)n * ntt, T.tt.begin());
-  std::copy(dtdq0, dtdq0 + n4, T.dtdq0.begin());
-  std::copy(dtdelements, dtdelements + n4, T.dtdelements.begin());
-  for (int q = 0; q < n; q++) T.count[q] = count[q];
-  T.s_prior.alloc(n);
-  intr_transits(s, T, h, tmax, grad != 0);
-  store_state(s, x, v, xerr, verr, jac_step, jac_err, dqdt);
-  *t = s.t;
-  std::copy(T.tt.begin(), T.tt.end(), tt);
-  std::copy(T.dtdq0.begin(), T.dtdq0.end(), dtdq0);
-  std::copy(T.dtdelements.begin(), T.dtdelements.end(), dtdelements);
-  for (int q = 0; q < n; q++) count[q] = T.count[q];
-  return 0;
+  return integrate_transits_nr<double>(1, n, ti, h, tmax, grad, t, x, v, m, xerr, verr, jac_step, jac_err, dqdt, pair,
+                               jac_init, ntt, tt, dtdq0, dtdelements, count);
+}
+
+// intr(s, ttbv::TransitParameters; grad) (Transits.jl:140-180 with the
+// TransitParameters branch of timing.jl:82-98): ttbv 3 x n x ntt,
+// dtbvdq0 / dtbvdelements 3 x n x ntt x 7 x n.
+int oracle_integrate_transit_parameters(int n, int ti, double h, double tmax, int grad, double* t, double* x,
+                                        double* v, const double* m, double* xerr, double* verr, double* jac_step,
+                                        double* jac_err, double* dqdt, const uint8_t* pair, const double* jac_init,
+                                        int ntt, double* ttbv, double* dtbvdq0, double* dtbvdelements,
+                                        int64_t* count) {
+  return integrate_transits_nr<double>(3, n, ti, h, tmax, grad, t, x, v, m, xerr, verr, jac_step, jac_err, dqdt,
+                                       pair, jac_init, ntt, ttbv, dtbvdq0, dtbvdelements, count);
+}
+
+// The same in quad precision (outputs rounded to double): the rounding-error
+// reference for the parity tolerances of the v_sky and b_sky^2 rows.
+int oracle_integrate_transit_parameters_quad(int n, int ti, double h, double tmax, int grad, double* t, double* x,
+                                             double* v, const double* m, double* xerr, double* verr,
+                                             double* jac_step, double* jac_err, double* dqdt, const uint8_t* pair,
+                                             const double* jac_init, int ntt, double* ttbv, double* dtbvdq0,
+                                             double* dtbvdelements, int64_t* count) {
+  return integrate_transits_nr<quad>(3, n, ti, h, tmax, grad, t, x, v, m, xerr, verr, jac_step, jac_err, dqdt,
+                                     pair, jac_init, ntt, ttbv, dtbvdq0, dtbvdelements, count);
 }
 
 // Batched CPU baseline: nsys independent systems of equal n, packed
@@ -362,14 +400,14 @@ int oracle_fd_dqdt(int n, double h, const double* x, const double* v, const doub
 // are perturbed by +-dq0 (absolute), initial conditions are recomputed with
 // init_nbody and the grad = false transit integration is repeated in quad.
 // H may be NULL (fully nested).  Output layout matches dtdelements.
-int oracle_fd_dtdelements(int n, double t0, const double* elements, const double* H, double h, double tmax,
-                          int ti, int ntt, double dq0_d, int nthreads, double* dtde_num) {
+static int fd_dtdelements_nr(int nr, int n, double t0, const double* elements, const double* H, double h,
+                             double tmax, int ti, int ntt, double dq0_d, int nthreads, double* dtde_num) {
   quad dq0 = quad(dq0_d);
   std::vector<quad> Hq((size_t)n * n), el0((size_t)n * 7);
   if (H) for (int q = 0; q < n * n; q++) Hq[q] = quad(H[q]);
   else hierarchy_nested<quad>(n, Hq.data());
   for (int q = 0; q < n * 7; q++) el0[q] = quad(elements[q]);
-  size_t n4 = (size_t)n * ntt * 7 * n;
+  size_t n4 = (size_t)nr * n * ntt * 7 * n;
   for (size_t q = 0; q < n4; q++) dtde_num[q] = 0.0;
   auto run = [&](int jq, int ivary, quad delta, TransitTiming<quad>& T) {
     std::vector<quad> el(el0);
@@ -379,7 +417,7 @@ int oracle_fd_dtdelements(int n, double t0, const double* elements, const double
     init_nbody<quad>(n, quad(t0), el.data(), Hq.data(), s.x.data(), s.v.data(), s.jac_init.data());
     for (int q = 0; q < n; q++) s.m[q] = el[q];
     s.t = quad(t0);
-    T.alloc(n, ntt, ti);
+    T.alloc(n, ntt, ti, nr);
     T.s_prior.alloc(n);
     intr_transits(s, T, quad(h), quad(tmax), false);
   };
@@ -395,8 +433,9 @@ int oracle_fd_dtdelements(int n, double t0, const double* elements, const double
       run(jq, ivary, -dq0, tm);
       for (int i : tm.occs)
         for (int64_t k = 0; k < tm.count[i] && k < ntt && k < tp.count[i]; k++)
-          dtde_num[tm.idx4(i, (int)k, iq, jq)] =
-              (double)((tp.tt[i + (size_t)n * k] - tm.tt[i + (size_t)n * k]) / (quad(2) * dq0));
+          for (int r = 0; r < nr; r++)
+            dtde_num[tm.idx4(i, (int)k, iq, jq, r)] =
+                (double)((tp.tt[tp.idx2(i, (int)k, r)] - tm.tt[tm.idx2(i, (int)k, r)]) / (quad(2) * dq0));
     }
   };
   std::vector<std::thread> th;
@@ -404,6 +443,18 @@ int oracle_fd_dtdelements(int n, double t0, const double* elements, const double
   work();
   for (auto& q : th) q.join();
   return 0;
+}
+
+int oracle_fd_dtdelements(int n, double t0, const double* elements, const double* H, double h, double tmax,
+                          int ti, int ntt, double dq0_d, int nthreads, double* dtde_num) {
+  return fd_dtdelements_nr(1, n, t0, elements, H, h, tmax, ti, ntt, dq0_d, nthreads, dtde_num);
+}
+
+// Numerical d(t, v_sky, b_sky^2) / d elements for TransitParameters
+// (test/test_transit_parameters.jl:47-82); layout of dtbvdelements.
+int oracle_fd_dtbvdelements(int n, double t0, const double* elements, const double* H, double h, double tmax,
+                            int ti, int ntt, double dq0_d, int nthreads, double* dtde_num) {
+  return fd_dtdelements_nr(3, n, t0, elements, H, h, tmax, ti, ntt, dq0_d, nthreads, dtde_num);
 }
 
 // Numerical jac_init (test/test_init_nbody.jl): two-sided differences in quad

@@ -1,31 +1,39 @@
 // nbg_oracle_transit.hpp -- TEST INFRASTRUCTURE ONLY (parity oracle; see
-// nbg_oracle.hpp).  Restates src/transits/Transits.jl:14-56,140-180 and
-// src/transits/timing.jl:3-123,141-193 for TransitTiming outputs, plus the
-// plain drivers of src/integrator/Integrator.jl:159-247.
+// nbg_oracle.hpp).  Restates src/transits/Transits.jl:14-110,140-180 and
+// src/transits/timing.jl:3-193 for TransitTiming and TransitParameters
+// outputs, plus the plain drivers of src/integrator/Integrator.jl:159-247.
 #pragma once
 
 namespace nbgo {
 
-// TransitTiming (Transits.jl:14-56).  Arrays are Julia column-major:
-//   tt[j + n c], dtdq0[j + n (c + ntt (k + 7 p))], dtdelements likewise.
+// TransitTiming (Transits.jl:14-56, nr = 1) and TransitParameters
+// (Transits.jl:68-110, nr = 3: rows t, v_sky, b_sky^2).  Arrays are Julia
+// column-major with the row index first:
+//   tt[r + nr (j + n c)], dtdq0[r + nr (j + n (c + ntt (k + 7 p)))],
+//   dtdelements likewise, dtdq[r + nr (k + 7 p)]; nr = 1 is TransitTiming's
+//   tt[j + n c], dtdq0[j + n (c + ntt (k + 7 p))].
 template <class T> struct TransitTiming {
   int n = 0, ntt = 0, ti = 0;  // ti is 0-based
+  int nr = 1;
   std::vector<T> tt, dtdq0, dtdelements, dtdq, gsave;
   std::vector<int64_t> count;
   std::vector<int> occs;
   State<T> s_prior, s_transit;
-  void alloc(int n_, int ntt_, int ti_) {
-    n = n_; ntt = ntt_; ti = ti_;
-    tt.assign((size_t)n * ntt, T(0));
-    dtdq0.assign((size_t)n * ntt * 7 * n, T(0));
-    dtdelements.assign((size_t)n * ntt * 7 * n, T(0));
-    dtdq.assign((size_t)7 * n, T(0));
+  void alloc(int n_, int ntt_, int ti_, int nr_ = 1) {
+    n = n_; ntt = ntt_; ti = ti_; nr = nr_;
+    tt.assign((size_t)nr * n * ntt, T(0));
+    dtdq0.assign((size_t)nr * n * ntt * 7 * n, T(0));
+    dtdelements.assign((size_t)nr * n * ntt * 7 * n, T(0));
+    dtdq.assign((size_t)nr * 7 * n, T(0));
     gsave.assign(n, T(0));
     count.assign(n, 0);
     occs.clear();
     for (int i = 0; i < n; i++) if (i != ti) occs.push_back(i);  // setdiff(1:n, ti)
   }
-  size_t idx4(int j, int c, int k, int p) const { return j + (size_t)n * (c + (size_t)ntt * (k + 7 * (size_t)p)); }
+  size_t idx4(int j, int c, int k, int p, int r = 0) const {
+    return r + (size_t)nr * (j + (size_t)n * (c + (size_t)ntt * (k + 7 * (size_t)p)));
+  }
+  size_t idx2(int j, int c, int r = 0) const { return r + (size_t)nr * (j + (size_t)n * c); }
 };
 
 // g! (timing.jl:141-144): sky-plane relative position dotted with velocity
@@ -56,6 +64,54 @@ template <class T> void dtbvdq1(State<T>& s, int i, int j, std::vector<T>& dtdq)
                         gd;
     }
   }
+}
+
+// calc_bsky2, calc_vsky (timing.jl:152-153)
+template <class T> T calc_bsky2(State<T>& s, int i, int j) {
+  return (s.X(0, j) - s.X(0, i)) * (s.X(0, j) - s.X(0, i)) + (s.X(1, j) - s.X(1, i)) * (s.X(1, j) - s.X(1, i));
+}
+template <class T> T calc_vsky(State<T>& s, int i, int j) {
+  return Mth<T>::sqrt((s.V(0, j) - s.V(0, i)) * (s.V(0, j) - s.V(0, i)) +
+                      (s.V(1, j) - s.V(1, i)) * (s.V(1, j) - s.V(1, i)));
+}
+
+// dtbvdq! with three rows (timing.jl:155-193): dtbvdq[r + 3 (k + 7 p)];
+// returns v_sky and b_sky^2.
+template <class T> void dtbvdq3(State<T>& s, int i, int j, std::vector<T>& dq, T* vsky_out, T* bsky2_out) {
+  T gd = gdot(s, i, j);
+  std::fill(dq.begin(), dq.end(), T(0));
+  int indj = 7 * j, indi = 7 * i;
+  for (int p = 0; p < s.n; p++) {
+    int indp = 7 * p;
+    for (int k = 0; k < 7; k++) {
+      int c = indp + k;
+      dq[0 + 3 * (k + 7 * p)] = -((s.J(indj, c) - s.J(indi, c)) * (s.V(0, j) - s.V(0, i)) +
+                                  (s.J(indj + 1, c) - s.J(indi + 1, c)) * (s.V(1, j) - s.V(1, i)) +
+                                  (s.J(indj + 3, c) - s.J(indi + 3, c)) * (s.X(0, j) - s.X(0, i)) +
+                                  (s.J(indj + 4, c) - s.J(indi + 4, c)) * (s.X(1, j) - s.X(1, i))) /
+                                gd;
+    }
+  }
+  T vsky = calc_vsky(s, i, j);
+  T bsky2 = calc_bsky2(s, i, j);
+  const std::vector<T>& q = s.dqdt;
+  T dvdt = ((s.V(0, j) - s.V(0, i)) * (q[7 * j + 3] - q[7 * i + 3]) +
+            (s.V(1, j) - s.V(1, i)) * (q[7 * j + 4] - q[7 * i + 4])) /
+           vsky;
+  for (int p = 0; p < s.n; p++) {
+    int indp = 7 * p;
+    for (int k = 0; k < 7; k++) {
+      int c = indp + k;
+      dq[1 + 3 * (k + 7 * p)] = ((s.J(indj + 3, c) - s.J(indi + 3, c)) * (s.V(0, j) - s.V(0, i)) +
+                                 (s.J(indj + 4, c) - s.J(indi + 4, c)) * (s.V(1, j) - s.V(1, i))) /
+                                    vsky +
+                                dvdt * dq[0 + 3 * (k + 7 * p)];
+      dq[2 + 3 * (k + 7 * p)] = T(2) * ((s.J(indj, c) - s.J(indi, c)) * (s.X(0, j) - s.X(0, i)) +
+                                        (s.J(indj + 1, c) - s.J(indi + 1, c)) * (s.X(1, j) - s.X(1, i)));
+    }
+  }
+  *vsky_out = vsky;
+  *bsky2_out = bsky2;
 }
 
 // Number of transit Newton searches that stopped at ITMAX (diagnostics only;
@@ -94,6 +150,24 @@ void findtransit(int i, int j, T dt0, State<T>& s, Derivs<T>& d, TransitTiming<T
     ahl21(s, d, dt0);
   }
   int64_t c = tt.count[j] - 1;
+  if (tt.nr == 3) {
+    // TransitParameters branch (timing.jl:82-98): t, v_sky, b_sky^2; without
+    // grad v_sky and b_sky^2 come from the last Newton iteration's state
+    tt.tt[tt.idx2(j, (int)c, 0)] = s.t + dt0;
+    if (grad) {
+      T vsky, bsky2;
+      dtbvdq3(s, i, j, tt.dtdq, &vsky, &bsky2);
+      tt.tt[tt.idx2(j, (int)c, 1)] = vsky;
+      tt.tt[tt.idx2(j, (int)c, 2)] = bsky2;
+      for (int r = 0; r < 3; r++)
+        for (int k = 0; k < 7; k++)
+          for (int p = 0; p < s.n; p++) tt.dtdq0[tt.idx4(j, (int)c, k, p, r)] = tt.dtdq[r + 3 * (k + 7 * p)];
+      return;
+    }
+    tt.tt[tt.idx2(j, (int)c, 1)] = calc_vsky(s, i, j);
+    tt.tt[tt.idx2(j, (int)c, 2)] = calc_bsky2(s, i, j);
+    return;
+  }
   tt.tt[j + (size_t)tt.n * c] = s.t + dt0;
   if (grad) {
     dtbvdq1(s, i, j, tt.dtdq);
@@ -123,21 +197,22 @@ template <class T> void detect_transits(State<T>& s, Derivs<T>& d, TransitTiming
   }
 }
 
-// calc_dtdelements! (timing.jl:112-123)
+// calc_dtdelements! (timing.jl:112-123; TransitParameters: :126-138, per row)
 template <class T> void calc_dtdelements(State<T>& s, TransitTiming<T>& tt) {
   int n = s.n, M = 7 * n;
-  for (int i = 0; i < n; i++)
-    for (int64_t j = 0; j < tt.count[i]; j++) {
-      if (j + 1 > tt.ntt) continue;
-      for (int k = 0; k < n; k++)
-        for (int l = 0; l < 7; l++) {
-          T acc = T(0);
-          for (int p = 0; p < n; p++)
-            for (int q = 0; q < 7; q++)
-              acc = acc + tt.dtdq0[tt.idx4(i, (int)j, q, p)] * s.jac_init[(7 * p + q) + (size_t)M * (7 * k + l)];
-          tt.dtdelements[tt.idx4(i, (int)j, l, k)] = acc;
-        }
-    }
+  for (int r = 0; r < tt.nr; r++)
+    for (int i = 0; i < n; i++)
+      for (int64_t j = 0; j < tt.count[i]; j++) {
+        if (j + 1 > tt.ntt) continue;
+        for (int k = 0; k < n; k++)
+          for (int l = 0; l < 7; l++) {
+            T acc = T(0);
+            for (int p = 0; p < n; p++)
+              for (int q = 0; q < 7; q++)
+                acc = acc + tt.dtdq0[tt.idx4(i, (int)j, q, p, r)] * s.jac_init[(7 * p + q) + (size_t)M * (7 * k + l)];
+            tt.dtdelements[tt.idx4(i, (int)j, l, k, r)] = acc;
+          }
+      }
 }
 
 // check_step (Integrator.jl:249-259)

@@ -111,6 +111,28 @@ def integrate_transits(s, tt, h, tmax, grad=True):
     assert rc == 0
 
 
+class OParams:
+    """TransitParameters (Transits.jl:68-110): ttbv 3 x n x ntt (t, v_sky, b_sky^2), dtbvdq0 and
+    dtbvdelements 3 x n x ntt x 7 x n."""
+
+    def __init__(self, n, ntt, ti=0):
+        self.n, self.ntt, self.ti = n, ntt, ti
+        self.ttbv = np.zeros((3, n, ntt), order="F")
+        self.dtbvdq0 = np.zeros((3, n, ntt, 7, n), order="F")
+        self.dtbvdelements = np.zeros((3, n, ntt, 7, n), order="F")
+        self.count = np.zeros(n, dtype=np.int64)
+
+
+def integrate_transit_parameters(s, tp, h, tmax, grad=True, quad=False):
+    """quad=True runs the same restatement in quad precision (outputs rounded to double)."""
+    fn = lib().oracle_integrate_transit_parameters_quad if quad else lib().oracle_integrate_transit_parameters
+    rc = fn(
+        s.n, tp.ti, ctypes.c_double(h), ctypes.c_double(tmax), int(grad), _p(s.t), _p(s.x), _p(s.v), _p(s.m),
+        _p(s.xerror), _p(s.verror), _p(s.jac_step), _p(s.jac_error), _p(s.dqdt), _p(s.pair, _U8), _p(s.jac_init),
+        tp.ntt, _p(tp.ttbv), _p(tp.dtbvdq0), _p(tp.dtbvdelements), _p(tp.count, _I64))
+    assert rc == 0
+
+
 def integrate_time(s, h, time, grad=True):
     rc = lib().oracle_integrate_time(
         s.n, ctypes.c_double(h), ctypes.c_double(time), int(grad), _p(s.t), _p(s.x), _p(s.v), _p(s.m),
@@ -196,6 +218,16 @@ def fd_dtdelements(elements, t0, h, tmax, ti, ntt, dq0=1e-10, H=None, nthreads=8
     Hm = None if H is None else f64(H)
     lib().oracle_fd_dtdelements(n, ctypes.c_double(t0), _p(el), _p(Hm), ctypes.c_double(h), ctypes.c_double(tmax),
                                 ti, ntt, ctypes.c_double(dq0), nthreads, _p(out))
+    return out
+
+
+def fd_dtbvdelements(elements, t0, h, tmax, ti, ntt, dq0=1e-10, H=None, nthreads=8):
+    el = f64(elements)
+    n = el.shape[0]
+    out = np.zeros((3, n, ntt, 7, n), order="F")
+    Hm = None if H is None else f64(H)
+    lib().oracle_fd_dtbvdelements(n, ctypes.c_double(t0), _p(el), _p(Hm), ctypes.c_double(h),
+                                  ctypes.c_double(tmax), ti, ntt, ctypes.c_double(dq0), nthreads, _p(out))
     return out
 
 

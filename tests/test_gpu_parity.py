@@ -288,3 +288,72 @@ def test_plain_integration_batch_is_bitwise_single():
         for k in ("x", "v", "jac_step", "dqdt"):
             assert np.array_equal(b.view(k, q), np.asarray(getattr(st, k)).ravel(order="F")), (q, k)
         assert b.view("t", q)[0] == st.t[0] == times[q]
+
+
+def _check_tbv(tp, to, tmax, grad, jac_init=None):
+    """TransitParameters parity: each row of ttbv and of the derivatives with the tolerances of
+    tests/parity.py (t: 1e-10 tmax absolute; v_sky, b_sky^2: 1e-10 relative to the row's scale)."""
+    P.check_counts(tp.count, to.count)
+    P.check_tt(tp.ttbv[0], to.ttbv[0], to.count, tmax)
+    for r in (1, 2):
+        for j, c in enumerate(to.count):
+            k = min(int(c), tp.ntt)
+            if k:
+                ref = to.ttbv[r, j, :k]
+                assert np.max(np.abs(tp.ttbv[r, j, :k] - ref)) <= 1e-10 * np.max(np.abs(ref)), (r, j)
+    if grad:
+        P.check_transit_derivs(tp.dtbvdq0[0], to.dtbvdq0[0], to.count, "dtbvdq0[0]")
+        P.check_transit_derivs(tp.dtbvdelements[0], to.dtbvdelements[0], to.count, "dtbvdelements[0]",
+                               to.dtbvdq0[0], jac_init)
+        for r in (1, 2):
+            P.check_rows_normwise(tp.dtbvdq0[r], to.dtbvdq0[r], to.count, "dtbvdq0[%d]" % r)
+            P.check_rows_normwise(tp.dtbvdelements[r], to.dtbvdelements[r], to.count, "dtbvdelements[%d]" % r)
+
+
+def _oracle_tbv(s, ic, n, ntt, h, tmax, grad):
+    so = O.OState(s.x.copy(order="F"), s.v.copy(order="F"), ic.m, jac_init=s.jac_init.copy(order="F"), t=0.0)
+    to = O.OParams(n, ntt, 0)
+    O.integrate_transit_parameters(so, to, h, tmax, grad=grad)
+    return so, to
+
+
+@pytest.mark.parametrize("grad", [True, False])
+@pytest.mark.parametrize("n", [3, 6])
+def test_transit_parameters_match_oracle(n, grad):
+    """intr(s, ttbv::TransitParameters; grad) (Transits.jl:68-110, timing.jl:82-98, :155-193)."""
+    els, hs, _ = W.batch_uneven(2, seed=80 + n, nmin=n, nmax=n)
+    el, h = els[1], hs[1]
+    tmax = 300 * h
+    ic = nbg.ElementsIC(0.0, n, el)
+    s = nbg.State(ic)
+    tp = nbg.TransitParameters(tmax, ic)
+    so, to = _oracle_tbv(s, ic, n, tp.ntt, h, tmax, grad)
+    nbg.Integrator(nbg.ahl21, h, 0.0, tmax)(s, tp, grad=grad)
+    assert to.count.sum() >= 2
+    _check_tbv(tp, to, tmax, grad, so.jac_init)
+    # t rows equal the TransitTiming call's tt bitwise; with grad, row 1 is its dtdq0
+    s2 = nbg.State(ic)
+    tt = nbg.TransitTiming(tmax, ic)
+    nbg.Integrator(nbg.ahl21, h, 0.0, tmax)(s2, tt, grad=grad)
+    assert np.array_equal(tt.tt, tp.ttbv[0]) and np.array_equal(tt.count, tp.count)
+    if grad:
+        assert np.array_equal(tt.dtdq0, tp.dtbvdq0[0])
+
+
+def test_transit_parameters_plain_3body_full_length():
+    """The plain 3-body configuration, 2000 steps and about 150 transits.  Its orbits are exactly
+    edge-on, so b_sky^2 and its derivatives are rounding noise (about 1e-18); the t and v_sky rows carry
+    the check."""
+    el, h, tmax = W.plain_3body(4)
+    ic = nbg.ElementsIC(0.0, 3, el)
+    s = nbg.State(ic)
+    tp = nbg.TransitParameters(tmax, ic)
+    so, to = _oracle_tbv(s, ic, 3, tp.ntt, h, tmax, True)
+    nbg.Integrator(nbg.ahl21, h, 0.0, tmax)(s, tp, grad=True)
+    assert to.count.sum() > 100
+    P.check_counts(tp.count, to.count)
+    P.check_tt(tp.ttbv[0], to.ttbv[0], to.count, tmax)
+    P.check_transit_derivs(tp.dtbvdq0[0], to.dtbvdq0[0], to.count, "dtbvdq0[0]")
+    P.check_rows_normwise(tp.dtbvdq0[1], to.dtbvdq0[1], to.count, "dtbvdq0[1]")
+    assert np.max(np.abs(tp.ttbv[2])) < 1e-12 and np.max(np.abs(tp.dtbvdq0[2])) < 1e-12
+    P.check_state(s, so)

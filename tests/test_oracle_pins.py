@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 
 import oracle_lib as O
+import parity as P
 from nbg import workloads as W
 
 close = O.maxabs_close
@@ -164,6 +165,71 @@ def test_transit_timing_derivatives(ref_elements):
     a, b = np.arcsinh(tt.dtdelements), np.arcsinh(num)
     assert close(a[mask], b[mask])
     assert close(a, b)
+
+
+def test_transit_parameters_derivatives(ref_elements):
+    """test/test_transit_parameters.jl: d(t, v_sky, b_sky^2)/d elements against quad
+    differences (h = 0.04, tmax = 10, dq0 = 1e-10), masked and unmasked."""
+    e, t0 = _transit_setup(ref_elements)
+    N, h, tmax = 3, 0.04, 10.0
+    x, v, jinit = O.init_nbody(e, t0)
+    ntt = O.ntt_for(tmax, e[:, 1])
+    s = O.OState(x, v, e[:, 0], jac_init=jinit, t=t0)
+    tp = O.OParams(N, ntt)
+    O.integrate_transit_parameters(s, tp, h, tmax, grad=True)
+    assert tp.count[1:].sum() >= 2
+    num = O.fd_dtbvdelements(e, t0, h, tmax, 0, ntt, dq0=1e-10)
+    mask = np.zeros(tp.dtbvdq0.shape, dtype=bool)
+    for jq in range(N):
+        for iq in range(7):
+            for i in range(1, N):
+                for k in range(tp.count[i]):
+                    if iq not in (4, 5) and not (jq == 0 and iq < 6) and not (jq == i and iq == 6):
+                        mask[:, i, k, iq, jq] = True
+    a, b = np.arcsinh(tp.dtbvdelements), np.arcsinh(num)
+    assert close(a[mask], b[mask])
+    assert close(a, b)
+
+
+def test_transit_parameters_times_equal_transit_timing(ref_elements):
+    """ttbv[1, :, :] of TransitParameters is TransitTiming's tt (same Newton search), with and without grad;
+    v_sky and b_sky^2 are those of the converged state."""
+    e, t0 = _transit_setup(ref_elements)
+    x, v, jinit = O.init_nbody(e, t0)
+    ntt = O.ntt_for(60.0, e[:, 1])
+    for grad in (True, False):
+        s1 = O.OState(x, v, e[:, 0], jac_init=jinit, t=t0)
+        s2 = O.OState(x, v, e[:, 0], jac_init=jinit, t=t0)
+        tt, tp = O.OTiming(3, ntt), O.OParams(3, ntt)
+        O.integrate_transits(s1, tt, 0.04, 60.0, grad=grad)
+        O.integrate_transit_parameters(s2, tp, 0.04, 60.0, grad=grad)
+        assert np.array_equal(tt.tt, tp.ttbv[0]) and np.array_equal(tt.count, tp.count)
+        if grad:
+            assert np.array_equal(tt.dtdq0, tp.dtbvdq0[0])
+        for i in range(1, 3):
+            k = int(tp.count[i])
+            assert np.all(tp.ttbv[1, i, :k] > 0) and np.all(tp.ttbv[2, i, :k] < 1.0)
+
+
+def test_transit_parameters_double_against_quad():
+    """The double-precision restatement of TransitParameters against the same code in quad precision
+    (100 steps, a mildly inclined 3-body system): the derivative rows agree normwise to 1e-8 of each
+    transit row (the rule the GPU parity tests apply to the v_sky and b_sky^2 rows)."""
+    els, hs, _ = W.batch_uneven(2, seed=83, nmin=3, nmax=3)
+    el, h = els[1], hs[1]
+    tmax = 100 * h
+    x, v, jinit = O.init_nbody(el, 0.0)
+    ntt = O.ntt_for(tmax, el[:, 1])
+    out = []
+    for quad in (False, True):
+        s = O.OState(x, v, el[:, 0], jac_init=jinit)
+        tp = O.OParams(3, ntt)
+        O.integrate_transit_parameters(s, tp, h, tmax, grad=True, quad=quad)
+        out.append(tp)
+    d, q = out
+    assert np.array_equal(d.count, q.count) and d.count.sum() >= 1
+    for r in range(3):
+        P.check_rows_normwise(d.dtbvdq0[r], q.dtbvdq0[r], d.count, "dtbvdq0[%d]" % r)
 
 
 def test_transit_times_grad_equals_nograd(ref_elements):
