@@ -138,6 +138,23 @@ int nbg_integrate_steps(nbg_context* ctx, int n, double h, int64_t nsteps, int g
                         double* jac_error, double* dqdt, const uint8_t* pair);
 
 /*
+ * init_nbody(ElementsIC(t0, H, elements)) for nsys systems on the GPU.
+ * Replaces src/ics/init_nbody.jl:13-229 (with kepler_init.jl:66-210 and
+ * kepler.jl:1-41) as called by State(ic) (src/integrator/Integrator.jl:82-103):
+ * elements is each system's N x 7 column-major ElementsIC.elements (m, P,
+ * t0, e cos w, e sin w, I, Omega), H its N x N hierarchy matrix (NULL: every
+ * system fully nested, hierarchy([N, 1, ..., 1])), t0 its epoch; out: x, v
+ * (3 x N) and jac_init (7N x 7N) per system, packed as the batched calls
+ * pack them.  The element checks of InitialConditions.jl:71-77 stay with the
+ * caller.  Host pointers (n, t0 always host).
+ */
+int nbg_batch_init_nbody(nbg_context* ctx, int nsys, const int32_t* n, const double* t0, const double* elements,
+                         const double* H, double* x, double* v, double* jac_init);
+/* The same with elements, H, x, v, jac_init in device memory. */
+int nbg_batch_init_nbody_device(nbg_context* ctx, int nsys, const int32_t* n, const double* t0,
+                                const double* elements, const double* H, double* x, double* v, double* jac_init);
+
+/*
  * Batched form: nsys independent systems integrated in one plan.  Each
  * system's arrays are laid out exactly as for nbg_integrate_transits and
  * concatenated system after system in every packed buffer (so the offset of

@@ -27,6 +27,7 @@ from .ics import CartesianIC, Elements, ElementsIC, hierarchy_nested, init_nbody
 __all__ = ["Elements", "ElementsIC", "CartesianIC", "State", "TransitTiming", "TransitParameters", "Integrator",
            "ahl21", "set_state",
            "Context", "NbgError", "default_context", "device_info", "integrate_transits_batch", "Batch", "Server",
+           "init_nbody_batch",
            "hierarchy_nested", "init_nbody", "kepler_init"]
 
 
@@ -389,6 +390,32 @@ class Server:
             self.stop()
         except Exception:
             pass
+
+
+def init_nbody_batch(ics, ctx=None):
+    """init_nbody for many ElementsIC on the GPU (nbg_batch_init_nbody): returns a list of
+    (x, v, jac_init) tuples, as ic.init_nbody() returns them on the host."""
+    ctx = ctx or default_context()
+    n = np.array([ic.nbody for ic in ics], dtype=np.int32)
+    t0 = np.array([ic.t0 for ic in ics], dtype=np.float64)
+    el = np.concatenate([np.asfortranarray(ic.elements, dtype=np.float64).ravel(order="F") for ic in ics])
+    nested = all(np.array_equal(ic.H, hierarchy_nested(ic.nbody)) for ic in ics)
+    H = None if nested else np.concatenate(
+        [np.asfortranarray(ic.H, dtype=np.float64).ravel(order="F") for ic in ics])
+    x = np.zeros(int(3 * n.sum()))
+    v = np.zeros(int(3 * n.sum()))
+    J = np.zeros(int((49 * n.astype(np.int64) ** 2).sum()))
+    p = _lib.ptr
+    _lib.check(_lib.load().nbg_batch_init_nbody(ctx.handle, len(ics), p(n, __import__("ctypes").POINTER(
+        __import__("ctypes").c_int32)), p(t0), p(el), p(H), p(x), p(v), p(J)))
+    out, ax, aJ = [], 0, 0
+    for k in n:
+        k = int(k)
+        out.append((x[ax:ax + 3 * k].reshape((3, k), order="F"), v[ax:ax + 3 * k].reshape((3, k), order="F"),
+                    J[aJ:aJ + 49 * k * k].reshape((7 * k, 7 * k), order="F")))
+        ax += 3 * k
+        aJ += 49 * k * k
+    return out
 
 
 def integrate_transits_batch(states, timings, h, tmax, grad=True, ctx=None):

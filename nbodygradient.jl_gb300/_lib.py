@@ -35,6 +35,7 @@ EXPORTS = (
     "nbg_batch_integrate_transits_noalloc",
     "nbg_integrate", "nbg_integrate_steps", "nbg_batch_integrate",
     "nbg_integrate_transit_parameters", "nbg_batch_integrate_transit_parameters",
+    "nbg_batch_init_nbody", "nbg_batch_init_nbody_device",
     "nbg_server_start", "nbg_server_enqueue", "nbg_server_wait_any", "nbg_server_poll", "nbg_server_stats",
     "nbg_server_stop",
 )
@@ -116,6 +117,9 @@ def load(build_if_missing=True):
     batch_args = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc), _D, _D, _D, _D, _D, _D, _D, _D, _D, _U8, _D, _D, _D,
                   _D, _I64, _U32]
     L.nbg_batch_integrate_transits.argtypes = batch_args
+    _I32 = ctypes.POINTER(ctypes.c_int32)
+    L.nbg_batch_init_nbody.argtypes = [_VP, ctypes.c_int, _I32, _D, _D, _D, _D, _D, _D]
+    L.nbg_batch_init_nbody_device.argtypes = [_VP, ctypes.c_int, _I32, _D] + [_VP] * 5
     L.nbg_batch_integrate_transit_parameters.argtypes = batch_args
     L.nbg_integrate_transit_parameters.argtypes = L.nbg_integrate_transits.argtypes
     L.nbg_batch_integrate_transits_device.argtypes = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc)] + [_VP] * 16

@@ -1,7 +1,7 @@
 """Builds libnbg_cuda.so (sm_103a) in-tree, under nbodygradient.jl_gb300/_build/.
 
 The library is one host/orchestration unit (csrc/nbg_cuda.cu), the request
-server (csrc/nbg_server.cu), the fixed scratch area of the allocation-free
+server (csrc/nbg_server.cu), the initial conditions (csrc/nbg_ics.cu), the fixed scratch area of the allocation-free
 entry point (csrc/nbg_noalloc.cu), and one
 kernel-instantiation unit per body count (csrc/nbg_inst.cu with -DNBG_N=2..10);
 the units compile in parallel and are linked with nvcc -shared.  A content
@@ -66,7 +66,8 @@ def build(force=False, verbose=False, jobs=None):
     nv = nvcc()
     units = [(os.path.join(CSRC, "nbg_cuda.cu"), os.path.join(BUILD_DIR, "nbg_cuda.o"), []),
              (os.path.join(CSRC, "nbg_noalloc.cu"), os.path.join(BUILD_DIR, "nbg_noalloc.o"), []),
-             (os.path.join(CSRC, "nbg_server.cu"), os.path.join(BUILD_DIR, "nbg_server.o"), [])]
+             (os.path.join(CSRC, "nbg_server.cu"), os.path.join(BUILD_DIR, "nbg_server.o"), []),
+             (os.path.join(CSRC, "nbg_ics.cu"), os.path.join(BUILD_DIR, "nbg_ics.o"), [])]
     for n in BODY_COUNTS:
         units.append((os.path.join(CSRC, "nbg_inst.cu"), os.path.join(BUILD_DIR, "nbg_inst_%d.o" % n),
                       ["-DNBG_N=%d" % n]))

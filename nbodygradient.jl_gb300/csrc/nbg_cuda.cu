@@ -1392,6 +1392,48 @@ int nbg_integrate_transits(nbg_context* ctx, int n, int ti, double h, double tma
                            dtdq0, dtdelements, count, nullptr, true);
 }
 
+static void* ctx_scratch(void* c, const char* name, size_t bytes) {
+  unsigned char* p = nullptr;
+  if (((nbg_context*)c)->get(name, bytes, &p)) return nullptr;
+  return p;
+}
+
+int nbg_batch_init_nbody_device(nbg_context* ctx, int nsys, const int32_t* n, const double* t0,
+                                const double* elements, const double* H, double* x, double* v, double* jac_init) {
+  if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
+  if (nsys <= 0 || !n || !t0 || !elements || !x || !v || !jac_init) return set_error(NBG_EINVAL, "NULL argument");
+  NBG_CUDA(cudaSetDevice(ctx->device));
+  return init_nbody_device(ctx->device, ctx->stream, nsys, n, t0, elements, H, x, v, jac_init, ctx_scratch, ctx);
+}
+
+int nbg_batch_init_nbody(nbg_context* ctx, int nsys, const int32_t* n, const double* t0, const double* elements,
+                         const double* H, double* x, double* v, double* jac_init) {
+  if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
+  if (nsys <= 0 || !n || !t0 || !elements || !x || !v || !jac_init) return set_error(NBG_EINVAL, "NULL argument");
+  NBG_CUDA(cudaSetDevice(ctx->device));
+  long long ael = 0, aH = 0, ax = 0, aJ = 0;
+  for (int s = 0; s < nsys; s++) {
+    if (n[s] < NBG_MIN_BODIES || n[s] > NBG_MAX_BODIES)
+      return set_error(NBG_EUNSUPPORTED, "system %d: n = %d outside %d..%d", s, n[s], NBG_MIN_BODIES, NBG_MAX_BODIES);
+    ael += 7LL * n[s]; aH += (long long)n[s] * n[s]; ax += 3LL * n[s]; aJ += 49LL * n[s] * n[s];
+  }
+  cudaStream_t st = ctx->stream;
+  double *d_el, *d_H = nullptr, *d_x, *d_v, *d_J;
+  int rc;
+  if ((rc = ctx->get("i_el", (size_t)ael, &d_el)) || (rc = ctx->get("i_x", (size_t)ax, &d_x)) ||
+      (rc = ctx->get("i_v", (size_t)ax, &d_v)) || (rc = ctx->get("i_J", (size_t)aJ, &d_J)))
+    return rc;
+  if (H && (rc = ctx->get("i_H", (size_t)aH, &d_H))) return rc;
+  NBG_CUDA(cudaMemcpyAsync(d_el, elements, sizeof(double) * ael, cudaMemcpyHostToDevice, st));
+  if (H) NBG_CUDA(cudaMemcpyAsync(d_H, H, sizeof(double) * aH, cudaMemcpyHostToDevice, st));
+  if ((rc = init_nbody_device(ctx->device, st, nsys, n, t0, d_el, d_H, d_x, d_v, d_J, ctx_scratch, ctx))) return rc;
+  NBG_CUDA(cudaMemcpyAsync(x, d_x, sizeof(double) * ax, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(v, d_v, sizeof(double) * ax, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaMemcpyAsync(jac_init, d_J, sizeof(double) * aJ, cudaMemcpyDeviceToHost, st));
+  NBG_CUDA(cudaStreamSynchronize(st));
+  return NBG_OK;
+}
+
 int nbg_integrate_transit_parameters(nbg_context* ctx, int n, int ti, double h, double tmax, int grad, double* t,
                                      double* x, double* v, const double* m, double* xerror, double* verror,
                                      double* jac_step, double* jac_error, double* dqdt, const uint8_t* pair,

@@ -57,6 +57,13 @@ void launch_unpack_jac(int N, int S, const int* sysidx, const SysOff* off, doubl
 void launch_dtdelements(int nlist, const int* list, const SysOff* off, const double* dtdq0, const double* jac_init,
                         double* dtdel, const long long* count, bool after_dtdq0, cudaStream_t st);
 
+// init_nbody for nsys systems on the device (nbg_ics.cu).  Array pointers
+// are device pointers (H may be null: fully nested hierarchies); n and t0
+// are host arrays.  get(ctx, name, bytes) returns device scratch.
+int init_nbody_device(int device, cudaStream_t st, int nsys, const int32_t* n, const double* t0,
+                      const double* d_elements, const double* d_H, double* d_x, double* d_v, double* d_jinit,
+                      void* (*get)(void* ctx, const char* name, size_t bytes), void* ctx);
+
 }  // namespace nbg
 
 #define NBG_CUDA(call)                                                                                    \
