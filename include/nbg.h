@@ -191,6 +191,21 @@ int nbg_batch_integrate_transit_parameters(nbg_context* ctx, int nsys, const nbg
                                            double* dtbvdelements, int64_t* count, uint32_t* status);
 
 /*
+ * (intr::Integrator)(s::State{Float64}, o::CartesianOutput{Float64})
+ * Replaces src/outputs/Outputs.jl:26-49: nstep steps (with gradient) of
+ * h * check_step(s.t, tmax), saving the state at the start of every step:
+ * out_t[i] = s.t + h i, out_x / out_v (3 x N per step) and, unless out_jac is
+ * NULL, out_jac (7N x 7N per step) -- the t, x, v and jac_step of
+ * o.states[i + 1].  The State is advanced in place; s.t = t0 + h nstep.  The
+ * records stream to the host chunk by chunk while the integration runs.  The
+ * reference's optional JLD2 file is the caller's to write.
+ */
+int nbg_integrate_cartesian(nbg_context* ctx, int n, double h, double tmax, int64_t nstep, double* t, double* x,
+                            double* v, const double* m, double* xerror, double* verror, double* jac_step,
+                            double* jac_error, double* dqdt, const uint8_t* pair, double* out_t, double* out_x,
+                            double* out_v, double* out_jac);
+
+/*
  * nbg_integrate for nsys systems in one plan: desc[s].tmax is system s's
  * target time (the `time` of intr(s, time)), desc[s].h its step and
  * desc[s].grad its flag (ti and ntt are ignored); arrays packed as for

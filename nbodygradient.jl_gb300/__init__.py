@@ -24,7 +24,8 @@ from . import _lib, build, workloads
 from ._lib import Context, NbgError, SystemDesc, default_context, device_info
 from .ics import CartesianIC, Elements, ElementsIC, hierarchy_nested, init_nbody, kepler_init
 
-__all__ = ["Elements", "ElementsIC", "CartesianIC", "State", "TransitTiming", "TransitParameters", "Integrator",
+__all__ = ["Elements", "ElementsIC", "CartesianIC", "State", "TransitTiming", "TransitParameters", "CartesianOutput",
+           "Integrator",
            "ahl21", "set_state",
            "Context", "NbgError", "default_context", "device_info", "integrate_transits_batch", "Batch", "Server",
            "init_nbody_batch",
@@ -135,6 +136,37 @@ class TransitParameters:
         self.count[...] = 0
 
 
+class CartesianOutput:
+    """Positions, velocities and Jacobian at every step (src/outputs/Outputs.jl:7-20).
+
+    After intr(s, o): o.t[i], o.x[i] (3 x N), o.v[i] and, with jac=True,
+    o.jac_step[i] (7N x 7N) hold the state at the start of step i + 1, as the
+    reference's o.states[i + 1].  The reference's JLD2 file output stays with
+    the caller (o.filename is kept for it)."""
+
+    def __init__(self, nbody, nstep, filename="data.jld2", file=False, jac=True):
+        self.nbody, self.nstep, self.filename, self.file = int(nbody), int(nstep), filename, file
+        n, M = self.nbody, 7 * self.nbody
+        self.t = np.zeros(self.nstep)
+        self.x = np.zeros((self.nstep, 3, n))
+        self.v = np.zeros((self.nstep, 3, n))
+        self.jac_step = np.zeros((self.nstep, M, M)) if jac else None
+
+    @property
+    def states(self):
+        """One lightweight record per saved step with t, x, v (and jac_step)."""
+        out = []
+        for i in range(self.nstep):
+            r = type("SavedState", (), {})()
+            r.t = np.array([self.t[i]])
+            r.x = np.asfortranarray(self.x[i])
+            r.v = np.asfortranarray(self.v[i])
+            if self.jac_step is not None:
+                r.jac_step = self.jac_step[i]
+            out.append(r)
+        return out
+
+
 class Integrator:
     """Integrator(scheme, h, t0, tmax) (src/integrator/Integrator.jl:17-31).
 
@@ -176,6 +208,23 @@ class Integrator:
                 _lib.check(L.nbg_integrate_steps(ctx.handle, s.n, self.h, int(tt), int(bool(grad)), *args))
             else:
                 _lib.check(L.nbg_integrate(ctx.handle, s.n, self.h, float(tt), int(bool(grad)), *args))
+            return None
+        if isinstance(tt, CartesianOutput):
+            if tt.nbody != s.n:
+                raise ValueError("CartesianOutput has %d bodies, the State %d" % (tt.nbody, s.n))
+            # C-order per-step blocks: step i's x is the column-major 3 x N block x_raw[i]
+            xr = np.zeros((tt.nstep, 3 * s.n))
+            vr = np.zeros((tt.nstep, 3 * s.n))
+            jr = None if tt.jac_step is None else np.zeros((tt.nstep, 49 * s.n * s.n))
+            _lib.check(L.nbg_integrate_cartesian(
+                ctx.handle, s.n, self.h, self.tmax, tt.nstep, p(s.t), p(s.x), p(s.v), p(s.m), p(s.xerror),
+                p(s.verror), p(s.jac_step), p(s.jac_error), p(s.dqdt), p(s.pair, _lib._U8), p(tt.t), p(xr), p(vr),
+                p(jr)))
+            for i in range(tt.nstep):
+                tt.x[i] = xr[i].reshape((3, s.n), order="F")
+                tt.v[i] = vr[i].reshape((3, s.n), order="F")
+                if jr is not None:
+                    tt.jac_step[i] = jr[i].reshape((7 * s.n, 7 * s.n), order="F")
             return None
         if isinstance(tt, TransitParameters):
             _lib.check(L.nbg_integrate_transit_parameters(

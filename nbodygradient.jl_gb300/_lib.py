@@ -35,7 +35,7 @@ EXPORTS = (
     "nbg_batch_integrate_transits_noalloc",
     "nbg_integrate", "nbg_integrate_steps", "nbg_batch_integrate",
     "nbg_integrate_transit_parameters", "nbg_batch_integrate_transit_parameters",
-    "nbg_batch_init_nbody", "nbg_batch_init_nbody_device",
+    "nbg_batch_init_nbody", "nbg_batch_init_nbody_device", "nbg_integrate_cartesian",
     "nbg_server_start", "nbg_server_enqueue", "nbg_server_wait_any", "nbg_server_poll", "nbg_server_stats",
     "nbg_server_stop",
 )
@@ -114,6 +114,8 @@ def load(build_if_missing=True):
     L.nbg_integrate.argtypes = [_VP, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int] + plain
     L.nbg_integrate_steps.argtypes = [_VP, ctypes.c_int, ctypes.c_double, ctypes.c_int64, ctypes.c_int] + plain
     L.nbg_batch_integrate.argtypes = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc)] + plain
+    L.nbg_integrate_cartesian.argtypes = [_VP, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int64] + \
+        plain + [_D, _D, _D, _D]
     batch_args = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc), _D, _D, _D, _D, _D, _D, _D, _D, _D, _U8, _D, _D, _D,
                   _D, _I64, _U32]
     L.nbg_batch_integrate_transits.argtypes = batch_args

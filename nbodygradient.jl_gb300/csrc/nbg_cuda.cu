@@ -338,6 +338,12 @@ struct PlainSpec {
   double tout;       // s.t after the call
 };
 
+// CartesianOutput destination of one system (host arrays, nsteps entries
+// each): t, x (3 x N), v (3 x N), jac_step (7N x 7N, may be null).
+struct TrajOut {
+  double *t, *x, *v, *jac;
+};
+
 struct GroupPlan {
   int N, grad;
   unsigned long long kick;
@@ -354,7 +360,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
               const uint8_t* pair_host, double* d_t, double* d_x, double* d_v, const double* d_m, double* d_xe,
               double* d_ve, double* d_J, double* d_E, double* d_dqdt, const double* d_jinit, double* d_tt,
               double* d_dq0, double* d_dtdel, long long* d_count, uint32_t* status_host,
-              const PlainSpec* plain = nullptr, int tbv = 0) {
+              const PlainSpec* plain = nullptr, int tbv = 0, const TrajOut* traj = nullptr) {
   const int nr = tbv ? 3 : 1;  // rows per transit of the outputs
   cudaStream_t st = ctx->stream;
   ctx->last_launches = 0;
@@ -486,6 +492,15 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     const size_t nsnap = (size_t)K * snap_count(gp.kick != 0) * 3 * N * S;
     const int nb = ctx->overlap ? 2 : 1;
     GET(task_f, nb * nf); GET(task_i, nb * ni); GET(task_count, nb);
+    size_t ntxv = 0, ntJ = 0;
+    if (traj) {
+      bool jac = false;
+      for (int q2 = 0; q2 < nsg; q2++) jac = jac || traj[gp.systems[q2]].jac;
+      ntxv = (size_t)S * K * 6 * N;
+      ntJ = jac ? (size_t)S * K * 49 * N * N : 0;
+      if ((rc = ctx->get(name("trajxv"), nb * ntxv, &g.trajxv))) return rc;
+      if (ntJ && (rc = ctx->get(name("trajJ"), nb * ntJ, &g.trajJ))) return rc;
+    }
     g.tgrid = std::min(((g.task_cap + 31) / 32) * 32, std::max(1, ctx->sm_count) * 4 * 32);
     if (gp.grad) {
       GET(steprec, nb * nrec); GET(trec, nb * ntrec); GET(tflag, nb * nflag); GET(tscratch, (size_t)g.R * g.tgrid);
@@ -529,6 +544,8 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     {
       GroupArgs h1 = g;
       h1.task_f += nf; h1.task_i += ni; h1.task_count += 1;
+      if (g.trajxv) h1.trajxv += ntxv;
+      if (g.trajJ) h1.trajJ += ntJ;
       if (gp.grad) { h1.steprec += nrec; h1.trec += ntrec; h1.tflag += nflag; h1.pcap += ncap; h1.xsnap += nsnap; }
       ghalf.push_back(h1);
     }
@@ -551,6 +568,34 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
   long long max_steps = 0;
   for (auto& kv : groups) max_steps = std::max(max_steps, kv.second.max_steps);
   const long long nchunks = (max_steps + K - 1) / K;
+  // CartesianOutput: after a chunk's consumer, its recorded states go to the
+  // callers' arrays (stream-ordered before the buffer half is reused)
+  std::vector<std::vector<std::pair<int, int>>> gtraj(gargs.size());  // (system, slot) per group
+  if (traj) {
+    int qg = 0;
+    for (auto& kv : groups) {
+      for (int q2 = 0; q2 < (int)kv.second.systems.size(); q2++) gtraj[qg].emplace_back(kv.second.systems[q2], q2);
+      qg++;
+    }
+  }
+  auto copy_traj = [&](size_t q, const GroupArgs& g, long long c, cudaStream_t s2) -> int {
+    if (!traj) return NBG_OK;
+    const int N = g.N, M = 7 * N;
+    for (auto& ss : gtraj[q]) {
+      const TrajOut& o = traj[ss.first];
+      const long long k0 = c * K, kn = std::min<long long>(K, nsteps[ss.first] - k0);
+      if (kn <= 0) continue;
+      const double* src = g.trajxv + (size_t)ss.second * K * 6 * N;
+      NBG_CUDA(cudaMemcpy2DAsync(o.x + k0 * 3 * N, sizeof(double) * 3 * N, src, sizeof(double) * 6 * N,
+                                 sizeof(double) * 3 * N, (size_t)kn, cudaMemcpyDeviceToHost, s2));
+      NBG_CUDA(cudaMemcpy2DAsync(o.v + k0 * 3 * N, sizeof(double) * 3 * N, src + 3 * N, sizeof(double) * 6 * N,
+                                 sizeof(double) * 3 * N, (size_t)kn, cudaMemcpyDeviceToHost, s2));
+      if (o.jac && g.trajJ)
+        NBG_CUDA(cudaMemcpyAsync(o.jac + k0 * M * M, g.trajJ + (size_t)ss.second * K * M * M,
+                                 sizeof(double) * kn * M * M, cudaMemcpyDeviceToHost, s2));
+    }
+    return NBG_OK;
+  };
   // profiling: an event pair around every orbit / Jacobian launch
   std::vector<std::pair<int, size_t>> prof;  // (kind, first event index)
   size_t nev = 0;
@@ -598,6 +643,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
           ctx->last_launches += 3;
           ctx->last_jac_launches++;
         }
+        if ((rc = copy_traj(q, g, c, st))) return rc;
       }
     }
   } else {
@@ -650,6 +696,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
         } else {
           NBG_CUDA(cudaStreamWaitEvent(sw, ev_tr, 0));
         }
+        if ((rc = copy_traj(q, g, c, sw))) return rc;
         NBG_CUDA(cudaEventRecord(ev_done, sw));
       }
     }
@@ -1255,7 +1302,7 @@ static int batch_host_device(nbg_context* ctx, int nsys, const nbg_system_desc* 
 // batched calls; no transit arrays).
 static int plain_host(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const PlainSpec* spec, double* t,
                       double* x, double* v, const double* m, double* xerror, double* verror, double* jac_step,
-                      double* jac_error, double* dqdt, const uint8_t* pair) {
+                      double* jac_error, double* dqdt, const uint8_t* pair, const TrajOut* traj = nullptr) {
   if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
   if (nsys <= 0 || !desc) return set_error(NBG_EINVAL, "nsys = %d", nsys);
   if (!t || !x || !v || !m || !xerror || !verror || !jac_step || !jac_error || !dqdt || !pair)
@@ -1287,7 +1334,7 @@ static int plain_host(nbg_context* ctx, int nsys, const nbg_system_desc* desc, c
   NBG_CUDA(cudaMemcpyAsync(d_dq, dqdt, sizeof(double) * adq, cudaMemcpyHostToDevice, st));
   NBG_CUDA(cudaMemsetAsync(d_cnt, 0, sizeof(long long) * am, st));
   rc = run_batch(ctx, nsys, desc, t, pair, d_t, d_x, d_v, d_m, d_xe, d_ve, d_J, d_E, d_dq, nullptr, nullptr, nullptr,
-                 nullptr, d_cnt, nullptr, spec);
+                 nullptr, d_cnt, nullptr, spec, 0, traj);
   if (rc) return rc;
   NBG_CUDA(cudaMemcpyAsync(t, d_t, sizeof(double) * nsys, cudaMemcpyDeviceToHost, st));
   NBG_CUDA(cudaMemcpyAsync(x, d_x, sizeof(double) * ax, cudaMemcpyDeviceToHost, st));
@@ -1357,6 +1404,30 @@ int nbg_integrate_steps(nbg_context* ctx, int n, double h, int64_t nsteps, int g
   nbg_system_desc d;
   d.n = n; d.ti = 0; d.grad = grad ? 1 : 0; d.ntt = 1; d.h = h; d.tmax = hs * (double)p.nsteps;
   return plain_host(ctx, 1, &d, &p, t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair);
+}
+
+int nbg_integrate_cartesian(nbg_context* ctx, int n, double h, double tmax, int64_t nstep, double* t, double* x,
+                            double* v, const double* m, double* xerror, double* verror, double* jac_step,
+                            double* jac_error, double* dqdt, const uint8_t* pair, double* out_t, double* out_x,
+                            double* out_v, double* out_jac) {
+  if (!t || !out_t || !out_x || !out_v) return set_error(NBG_EINVAL, "NULL array argument");
+  if (!(h != 0.0) || !std::isfinite(h) || !std::isfinite(tmax) || !std::isfinite(t[0]))
+    return set_error(NBG_EINVAL, "h = %g, tmax = %g", h, tmax);
+  if (nstep < 0 || nstep > (1LL << 32)) return set_error(NBG_EINVAL, "nstep = %lld", (long long)nstep);
+  // (intr::Integrator)(s, o::CartesianOutput) (Outputs.jl:26-49): nstep grad
+  // steps of h * check_step(t0, intr.tmax); the state before step i is saved,
+  // with s.t = t0 + h (i - 1); afterwards s.t = t0 + h nstep
+  const double t0 = t[0];
+  PlainSpec p;
+  p.h = h * check_step(t0, tmax);
+  p.hlast = p.h;
+  p.nsteps = nstep;
+  p.tout = nstep > 0 ? t0 + (p.h * (double)nstep) : t0;
+  for (long long i = 0; i < nstep; i++) out_t[i] = (i == 0) ? t0 : t0 + (p.h * (double)i);
+  nbg_system_desc d;
+  d.n = n; d.ti = 0; d.grad = 1; d.ntt = 1; d.h = h; d.tmax = tmax;
+  TrajOut o{out_t, out_x, out_v, out_jac};
+  return plain_host(ctx, 1, &d, &p, t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair, &o);
 }
 
 int nbg_batch_integrate(nbg_context* ctx, int nsys, const nbg_system_desc* desc, double* t, double* x, double* v,

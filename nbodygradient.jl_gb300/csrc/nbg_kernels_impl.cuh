@@ -52,6 +52,13 @@ __global__ void __launch_bounds__(PROD_BS) orbit_chunk_kernel(GroupArgs g, int c
     const long long istep = k0 + kk;
     if (istep >= nst) break;
     const double hs = step_length(g, s, istep, nst, h);
+    if (g.trajxv) {
+      double* rx = g.trajxv + ((size_t)s * g.K + kk) * 6 * N;
+      for (int q = 0; q < 3 * N; q++) {
+        rx[q] = st.x[q];
+        rx[3 * N + q] = st.v[q];
+      }
+    }
     if (g.grad) {
       // x, v only; the operators are built from the captures by the operator
       // kernels.  The last step also computes dq/dt, the State's output.
@@ -332,6 +339,10 @@ __global__ void __launch_bounds__(CONS_BS) jacobian_chunk_kernel(GroupArgs g, in
     const long long istep = k0 + kk;
     if (istep >= nst) break;
     Rec rec{g.steprec + (size_t)kk * g.R * S + s, S};
+    if (g.trajJ) {  // column c of jac_step at the start of the step; mass rows are unit rows
+      double* rj = g.trajJ + (((size_t)s * g.K + kk) * M + c) * M;
+      for (int r = 0; r < M; r++) rj[r] = (r % 7 == 6) ? ((r == c) ? 1.0 : 0.0) : J[(6 * (r / 7) + r % 7) * CONS_BS];
+    }
     apply_step<N, CONS_BS>(J, E, c, step_length(g, s, istep, nst, h), kick, rec);
     if (g.notransit) continue;
     for (int o = 0; o < N - 1; o++) {

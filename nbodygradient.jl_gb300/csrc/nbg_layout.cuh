@@ -57,6 +57,11 @@ struct GroupArgs {
   const double* hlast;
   int notransit;  // 1: no transit detection (the plain integration drivers)
   int tbv;        // 1: TransitParameters outputs (t, v_sky, b_sky^2 per transit)
+  // CartesianOutput recording (null: off): the state at the start of every
+  // step of the chunk, x and v as [slot][step][x (3N), v (3N)], jac_step as
+  // [slot][step][7N x 7N column-major]
+  double* trajxv;
+  double* trajJ;
   int *ntt, *ti, *sysidx;
   unsigned int* status;
   // packed outputs in the caller's layout, indexed by global system

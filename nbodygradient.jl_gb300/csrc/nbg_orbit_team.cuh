@@ -177,6 +177,13 @@ __global__ void __launch_bounds__(PROD_BS) orbit_team_kernel(GroupArgs g, int ch
       xs = Rec{g.xsnap + (size_t)kk * snap_count(false) * 3 * N * S + s, S};
     }
     const double hs = run ? step_length(g, s, istep, nst, h) : h;
+    if (run && g.trajxv) {
+      double* rx = g.trajxv + ((size_t)s * g.K + kk) * 6 * N;
+      for (int q = t; q < 3 * N; q += L) {
+        rx[q] = st.x[q];
+        rx[3 * N + q] = st.v[q];
+      }
+    }
     team_step<N>(st, acc[tm], w, t, run && !last, hs, cap, xs);
     // the last step also forms dq/dt: the one-lane step, on the team's first lane
     if (last && t == 0) ahl21_step<N, true, true>(st, w, hs, 0, Rec{nullptr, 0}, cap, xs);

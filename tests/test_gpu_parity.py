@@ -357,3 +357,31 @@ def test_transit_parameters_plain_3body_full_length():
     P.check_rows_normwise(tp.dtbvdq0[1], to.dtbvdq0[1], to.count, "dtbvdq0[1]")
     assert np.max(np.abs(tp.ttbv[2])) < 1e-12 and np.max(np.abs(tp.dtbvdq0[2])) < 1e-12
     P.check_state(s, so)
+
+
+@pytest.mark.parametrize("n", [3, 7])
+def test_cartesian_output_trajectory(n):
+    """intr(s, o::CartesianOutput) (Outputs.jl:26-49): the state saved at the start of every step
+    against the oracle stepping one step at a time, and the final state bitwise that of intr(s, N)."""
+    els, hs, _ = W.batch_uneven(2, seed=90 + n, nmin=n, nmax=n)
+    el, h = els[0], hs[0]
+    nstep = 150  # more than two chunks
+    ic = nbg.ElementsIC(0.0, n, el)
+    s = nbg.State(ic)
+    s2 = s.copy()
+    o = nbg.CartesianOutput(n, nstep)
+    intr = nbg.Integrator(nbg.ahl21, h, 0.0, 1e4)
+    intr(s, o)
+    nbg.Integrator(nbg.ahl21, h, 0.0, 1e4)(s2, nstep)
+    for k in ("x", "v", "jac_step", "dqdt"):
+        assert np.array_equal(getattr(s, k), getattr(s2, k)), k
+    assert s.t[0] == s2.t[0]
+    so = O.OState(ic.init_nbody()[0], ic.init_nbody()[1], ic.m, jac_init=s.jac_init.copy(order="F"), t=0.0)
+    for i in range(nstep):
+        assert o.t[i] == (0.0 if i == 0 else 0.0 + h * i)
+        for k in ("x", "v"):
+            ref = getattr(so, k)
+            assert np.max(np.abs(getattr(o, k)[i] - ref)) <= 1e-10 * np.max(np.abs(ref)), (i, k)
+        colmax = np.max(np.abs(so.jac_step), axis=0, keepdims=True)
+        assert np.all(np.abs(o.jac_step[i] - so.jac_step) <= 1e-9 * (np.abs(so.jac_step) + 1e-4 * colmax)), i
+        O.integrate_nsteps(so, h, 1)
