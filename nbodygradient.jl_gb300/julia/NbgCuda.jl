@@ -1,18 +1,23 @@
 # NbgCuda.jl -- routes NbodyGradient.jl's transit-timing integration through
 # libnbg_cuda (the GB300 implementation of this package).
 #
-# Loading this file after `using NbodyGradient` adds a method, more specific
-# than (intr::Integrator)(s::State, tt::TransitOutput; grad, return_arrays)
-# (src/transits/Transits.jl:173-180), for Float64 states, TransitTiming
-# outputs and the ahl21! scheme.  Everything else stays on the reference's
-# own code path.  The library path comes from ENV["NBG_CUDA_LIB"].
+# Loading this file after `using NbodyGradient` adds methods, more specific
+# than the reference's, for Float64 states and the ahl21! scheme:
+#   intr(s, tt::TransitTiming; grad)        (src/transits/Transits.jl:173-180)
+#   intr(s, ttbv::TransitParameters; grad)  (same, TransitParameters output)
+#   intr(s, time::Float64; grad)            (src/integrator/Integrator.jl:159)
+#   intr(s, N::Int64; grad)                 (src/integrator/Integrator.jl:210)
+#   intr(s, o::CartesianOutput)             (src/outputs/Outputs.jl:26)
+# (intr(s; grad) reaches the GPU through intr(s, time).)  Everything else
+# stays on the reference's own code path.  The library path comes from
+# ENV["NBG_CUDA_LIB"].
 #
 # Not exercised in this repository's test suite (Julia is not installed on
 # the build and GPU hosts); tests drive the same C ABI from Python.
 module NbgCuda
 
 using NbodyGradient
-import NbodyGradient: Integrator, State, TransitTiming, ahl21!
+import NbodyGradient: Integrator, State, TransitTiming, TransitParameters, CartesianOutput, ahl21!, check_step
 
 const LIB = get(ENV, "NBG_CUDA_LIB", "libnbg_cuda.so")
 const CTX = Ref{Ptr{Cvoid}}(C_NULL)
@@ -50,6 +55,71 @@ function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, tt::Trans
     rc == 0 || error("libnbg_cuda: ", last_error())
     return_arrays && return nothing  # no Derivatives scratch exists on this path
     return nothing
+end
+
+function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, ttbv::TransitParameters{Float64};
+                                                    grad::Bool=true, return_arrays::Bool=false)
+    GC.@preserve s ttbv begin
+        rc = ccall((:nbg_integrate_transit_parameters, LIB), Cint,
+                   (Ptr{Cvoid}, Cint, Cint, Cdouble, Cdouble, Cint,
+                    Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+                    Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Bool}, Ptr{Float64}, Int64,
+                    Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Int64}),
+                   context(), s.n, ttbv.ti - 1, intr.h, intr.tmax, grad ? 1 : 0,
+                   s.t, s.x, s.v, s.m, s.xerror, s.verror,
+                   s.jac_step, s.jac_error, s.dqdt, s.pair, s.jac_init, ttbv.ntt,
+                   ttbv.ttbv, ttbv.dtbvdq0, ttbv.dtbvdelements, ttbv.count)
+    end
+    rc == 0 || error("libnbg_cuda: ", last_error())
+    return nothing
+end
+
+const PLAIN_ARGS = (Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+                    Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Bool})
+
+function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, time::Float64; grad::Bool=true)
+    GC.@preserve s begin
+        rc = ccall((:nbg_integrate, LIB), Cint,
+                   (Ptr{Cvoid}, Cint, Cdouble, Cdouble, Cint, PLAIN_ARGS...),
+                   context(), s.n, intr.h, time, grad ? 1 : 0,
+                   s.t, s.x, s.v, s.m, s.xerror, s.verror, s.jac_step, s.jac_error, s.dqdt, s.pair)
+    end
+    rc == 0 || error("libnbg_cuda: ", last_error())
+    return
+end
+
+function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, N::Int64; grad::Bool=true)
+    GC.@preserve s begin
+        rc = ccall((:nbg_integrate_steps, LIB), Cint,
+                   (Ptr{Cvoid}, Cint, Cdouble, Int64, Cint, PLAIN_ARGS...),
+                   context(), s.n, intr.h, N, grad ? 1 : 0,
+                   s.t, s.x, s.v, s.m, s.xerror, s.verror, s.jac_step, s.jac_error, s.dqdt, s.pair)
+    end
+    rc == 0 || error("libnbg_cuda: ", last_error())
+    return
+end
+
+function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, o::CartesianOutput{Float64})
+    n, M, nstep = s.n, 7 * s.n, o.nstep
+    ts = Vector{Float64}(undef, nstep)
+    xs = Array{Float64}(undef, 3, n, nstep)
+    vs = Array{Float64}(undef, 3, n, nstep)
+    js = Array{Float64}(undef, M, M, nstep)
+    GC.@preserve s begin
+        rc = ccall((:nbg_integrate_cartesian, LIB), Cint,
+                   (Ptr{Cvoid}, Cint, Cdouble, Cdouble, Int64, PLAIN_ARGS...,
+                    Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                   context(), n, intr.h, intr.tmax, nstep,
+                   s.t, s.x, s.v, s.m, s.xerror, s.verror, s.jac_step, s.jac_error, s.dqdt, s.pair,
+                   ts, xs, vs, js)
+    end
+    rc == 0 || error("libnbg_cuda: ", last_error())
+    for i in 1:nstep  # o.states[i] = the state before step i (Outputs.jl:38-40)
+        si = deepcopy(s)
+        si.t[1] = ts[i]; si.x .= xs[:, :, i]; si.v .= vs[:, :, i]; si.jac_step .= js[:, :, i]
+        o.states[i] = si
+    end
+    return
 end
 
 end # module
