@@ -74,13 +74,14 @@ function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, ttbv::Tra
     return nothing
 end
 
-const PLAIN_ARGS = (Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
-                    Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Bool})
-
+# ccall's argument types must be a literal tuple, so the State pointers
+# (t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair) are spelled out.
 function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, time::Float64; grad::Bool=true)
     GC.@preserve s begin
         rc = ccall((:nbg_integrate, LIB), Cint,
-                   (Ptr{Cvoid}, Cint, Cdouble, Cdouble, Cint, PLAIN_ARGS...),
+                   (Ptr{Cvoid}, Cint, Cdouble, Cdouble, Cint,
+                    Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+                    Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Bool}),
                    context(), s.n, intr.h, time, grad ? 1 : 0,
                    s.t, s.x, s.v, s.m, s.xerror, s.verror, s.jac_step, s.jac_error, s.dqdt, s.pair)
     end
@@ -91,7 +92,9 @@ end
 function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, N::Int64; grad::Bool=true)
     GC.@preserve s begin
         rc = ccall((:nbg_integrate_steps, LIB), Cint,
-                   (Ptr{Cvoid}, Cint, Cdouble, Int64, Cint, PLAIN_ARGS...),
+                   (Ptr{Cvoid}, Cint, Cdouble, Int64, Cint,
+                    Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+                    Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Bool}),
                    context(), s.n, intr.h, N, grad ? 1 : 0,
                    s.t, s.x, s.v, s.m, s.xerror, s.verror, s.jac_step, s.jac_error, s.dqdt, s.pair)
     end
@@ -107,7 +110,9 @@ function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, o::Cartes
     js = Array{Float64}(undef, M, M, nstep)
     GC.@preserve s begin
         rc = ccall((:nbg_integrate_cartesian, LIB), Cint,
-                   (Ptr{Cvoid}, Cint, Cdouble, Cdouble, Int64, PLAIN_ARGS...,
+                   (Ptr{Cvoid}, Cint, Cdouble, Cdouble, Int64,
+                    Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+                    Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Bool},
                     Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
                    context(), n, intr.h, intr.tmax, nstep,
                    s.t, s.x, s.v, s.m, s.xerror, s.verror, s.jac_step, s.jac_error, s.dqdt, s.pair,
