@@ -350,6 +350,9 @@ def main():
     ap.add_argument("--orbit-team", type=int, default=-1,
                     help="orbit producer form: -1 automatic, 0 one lane per system, 1 a team per system")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip the autotuner (it picks chunk length and orbit-producer mapping before the warm-up)")
+    ap.add_argument("--tune-steps", type=int, default=256, help="steps per system of each autotuner trial")
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--serve", action="store_true", help="serving (C4): Poisson request streams, then exit")
@@ -399,6 +402,12 @@ def main():
     def reset():
         for k in dev:
             dev[k].copy_(dev0[k])
+
+    tuning = None
+    if not args.no_autotune and not (args.chunk or args.serial or args.spw or args.orbit_team != -1):
+        reset()
+        tuning = b.autotune_device(dev, ctx, trial_steps=args.tune_steps)
+        chunk = tuning[0]["chunk_steps"]
 
     def step():
         reset()
@@ -484,8 +493,17 @@ def main():
             "config": {"workload": args.workload, "nsys": len(states), "system_steps_per_pass": total_ss,
                        "grad": True, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "working set larger than L2 (operator records + jac_step)",
-                       "chunk_steps": chunk, "orbit_systems_per_warp": args.spw or "auto",
-                       "orbit_team": {-1: "auto", 0: "off", 1: "on"}[args.orbit_team],
+                       "chunk_steps": chunk,
+                       "orbit_systems_per_warp": (args.spw or "auto") if tuning is None
+                       else (tuning[0]["orbit_lanes"] or "auto"),
+                       "orbit_team": ({-1: "auto", 0: "off", 1: "on"}[args.orbit_team] if tuning is None
+                                      else {0: "off", 1: "on"}[tuning[0]["orbit_team"]]),
+                       "autotuner": None if tuning is None else {
+                           "trial_steps_per_system": args.tune_steps,
+                           "chosen": {k: tuning[0][k] for k in ("chunk_steps", "orbit_team", "orbit_lanes")},
+                           "candidates": [{k: (round(r[k], 2) if k == "ms" else r[k])
+                                           for k in ("chunk_steps", "orbit_team", "orbit_lanes", "ms")}
+                                          for r in tuning]},
                        "streams": 1 if args.serial else 3},
             "e2e": {"value": e2e_val, "unit": "system-steps/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.mean(e2e_ms)) if e2e_ms else None},

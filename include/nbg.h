@@ -361,6 +361,30 @@ int nbg_set_tuning(nbg_context* ctx, int chunk_steps, int overlap);
  * search and Jacobian-consumer launches.  No counterpart in the reference. */
 int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double* transit_ms, double* jacobian_ms);
 
+/*
+ * Autotuner (no counterpart in the reference).  Times two short trial
+ * integrations of this batch -- every system's first min(nsteps, T) steps
+ * for T = trial_steps and 2 trial_steps, on device copies (the caller's
+ * arrays are not modified) -- for each candidate mapping: steps per chunk
+ * {32, 64, 128} x orbit producer form {one lane per system, team of lanes} x
+ * producer systems per warp {automatic, 16}.  The two trial times extrapolate
+ * the chunk loop's time to the batch's longest system (pipeline fill and
+ * drain plus a steady cost per step); the fastest candidate is kept on the
+ * context (as nbg_set_tuning / nbg_set_orbit_team / nbg_set_orbit_lanes
+ * would).  Arrays as for nbg_batch_integrate_transits_device.  report (may
+ * be NULL) receives up to report_len candidates; *nreport (may be NULL)
+ * their number.  Results of later calls do not depend on the choice.
+ */
+typedef struct {
+  int32_t chunk_steps, orbit_team, orbit_lanes, pad;
+  double ms;                 /* predicted chunk-loop time of the full batch   */
+  double system_steps_per_s; /* the batch's system-steps / that time          */
+} nbg_tuning_result;
+int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc_host, double* t, double* x, double* v,
+                        const double* m, double* xerror, double* verror, double* jac_step, double* jac_error,
+                        double* dqdt, const uint8_t* pair, const double* jac_init, int trial_steps,
+                        nbg_tuning_result* report, int report_len, int* nreport);
+
 /* Systems per warp of the orbit producer (1..32; 0 = automatic: about two
  * warps per SM).  A tuning knob; results do not depend on it. */
 int nbg_set_orbit_lanes(nbg_context* ctx, int systems_per_warp);

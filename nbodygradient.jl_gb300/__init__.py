@@ -350,6 +350,24 @@ class Batch:
             vp("dtdq0"), vp("dtdelements"), vp("count"), __import__("ctypes").c_void_p(self.status.ctypes.data)))
         return self
 
+    def autotune_device(self, dev_arrays, ctx=None, trial_steps=256):
+        """nbg_autotune_device on device buffers: picks the fastest mapping for this batch on ctx and
+        returns the candidates' trial timings (a list of dicts, the chosen one first)."""
+        import ctypes
+        ctx = ctx or default_context()
+        L = _lib.load()
+        d = dev_arrays
+        vp = lambda k: ctypes.c_void_p(d[k].data_ptr())
+        rep = (_lib.TuningResult * 32)()
+        nrep = ctypes.c_int(0)
+        _lib.check(L.nbg_autotune_device(
+            ctx.handle, self.nsys, self.descriptors(), vp("t"), vp("x"), vp("v"), vp("m"), vp("xerror"),
+            vp("verror"), vp("jac_step"), vp("jac_error"), vp("dqdt"), vp("pair"), vp("jac_init"), int(trial_steps),
+            rep, 32, ctypes.byref(nrep)))
+        out = [{k: getattr(rep[q], k) for k, _ in _lib.TuningResult._fields_ if k != "pad"}
+               for q in range(nrep.value)]
+        return sorted(out, key=lambda r: r["ms"])
+
     def run_device_noalloc(self, dev_arrays, ctx=None):
         """nbg_batch_integrate_transits_noalloc on device buffers: the same call
         with every working buffer taken from the library's fixed scratch array

@@ -35,7 +35,7 @@ EXPORTS = (
     "nbg_batch_integrate_transits_noalloc",
     "nbg_integrate", "nbg_integrate_steps", "nbg_batch_integrate",
     "nbg_integrate_transit_parameters", "nbg_batch_integrate_transit_parameters",
-    "nbg_batch_init_nbody", "nbg_batch_init_nbody_device", "nbg_integrate_cartesian",
+    "nbg_batch_init_nbody", "nbg_batch_init_nbody_device", "nbg_integrate_cartesian", "nbg_autotune_device",
     "nbg_server_start", "nbg_server_enqueue", "nbg_server_wait_any", "nbg_server_poll", "nbg_server_stats",
     "nbg_server_stop",
 )
@@ -56,6 +56,11 @@ class DeviceInfo(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char * 128), ("sm_count", ctypes.c_int), ("cc_major", ctypes.c_int),
                 ("cc_minor", ctypes.c_int), ("total_mem", ctypes.c_size_t), ("min_bodies", ctypes.c_int),
                 ("max_bodies", ctypes.c_int)]
+
+
+class TuningResult(ctypes.Structure):
+    _fields_ = [("chunk_steps", ctypes.c_int32), ("orbit_team", ctypes.c_int32), ("orbit_lanes", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("ms", ctypes.c_double), ("system_steps_per_s", ctypes.c_double)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -126,6 +131,8 @@ def load(build_if_missing=True):
     L.nbg_integrate_transit_parameters.argtypes = L.nbg_integrate_transits.argtypes
     L.nbg_batch_integrate_transits_device.argtypes = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc)] + [_VP] * 16
     L.nbg_batch_integrate_transits_noalloc.argtypes = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc)] + [_VP] * 16
+    L.nbg_autotune_device.argtypes = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc)] + [_VP] * 11 + \
+        [ctypes.c_int, ctypes.POINTER(TuningResult), ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     L.nbg_set_tuning.argtypes = [_VP, ctypes.c_int, ctypes.c_int]
     L.nbg_last_timing.argtypes = [_VP, _D, _D, _D, _D]
     L.nbg_last_launch_count.argtypes = [_VP]

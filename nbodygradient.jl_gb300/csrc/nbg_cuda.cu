@@ -1563,6 +1563,135 @@ int nbg_batch_integrate_transits_device(nbg_context* ctx, int nsys, const nbg_sy
                    jac_init, tt, dtdq0, dtdelements, (long long*)count, status);
 }
 
+int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc, double* t, double* x, double* v,
+                        const double* m, double* xerror, double* verror, double* jac_step, double* jac_error,
+                        double* dqdt, const uint8_t* pair, const double* jac_init, int trial_steps,
+                        nbg_tuning_result* report, int report_len, int* nreport) {
+  if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
+  if (nsys <= 0 || !desc) return set_error(NBG_EINVAL, "nsys = %d", nsys);
+  if (trial_steps < 8 || trial_steps > 100000) return set_error(NBG_EINVAL, "trial_steps = %d", trial_steps);
+  NBG_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  // two trials per candidate: every system's first min(nsteps, T) steps for
+  // T = trial_steps and 2 trial_steps, on copies.  The loop time is close to
+  // affine in T (pipeline fill and drain, then a steady cost per step), so the
+  // two trials extrapolate it to the batch's longest system.
+  std::vector<nbg_system_desc> td1(desc, desc + nsys), td2(desc, desc + nsys);
+  long long ax = 0, am = 0, aJ = 0, adq = 0, ap = 0, att = 0, adq0 = 0, steps = 0, longest = 0;
+  bool any_team = false;
+  for (int s = 0; s < nsys; s++) {
+    const int n = desc[s].n, M = 7 * n;
+    if (n < NBG_MIN_BODIES || n > NBG_MAX_BODIES) return set_error(NBG_EUNSUPPORTED, "system %d: n = %d", s, n);
+    if (!(desc[s].h != 0.0) || !std::isfinite(desc[s].h) || !std::isfinite(desc[s].tmax) || desc[s].ntt < 1)
+      return set_error(NBG_EINVAL, "system %d: h = %g, tmax = %g, ntt = %d", s, desc[s].h, desc[s].tmax, desc[s].ntt);
+    const long long full = steps_of(desc[s].h, desc[s].tmax);
+    const double sg = desc[s].tmax < 0 ? -1.0 : 1.0;
+    td1[s].tmax = sg * std::fabs(desc[s].h) * (double)std::min<long long>(full, trial_steps);
+    td2[s].tmax = sg * std::fabs(desc[s].h) * (double)std::min<long long>(full, 2LL * trial_steps);
+    steps += full;
+    longest = std::max(longest, full);
+    any_team = any_team || n >= 4;
+    ax += 3 * n; am += n; aJ += (long long)M * M; adq += M; ap += (long long)n * n;
+    att += (long long)n * desc[s].ntt; adq0 += (long long)n * desc[s].ntt * 7 * n;
+  }
+  if (steps == 0) return set_error(NBG_EINVAL, "the batch has no steps to time");
+  std::vector<double> th(nsys);
+  std::vector<uint8_t> ph(ap);
+  NBG_CUDA(cudaMemcpy(th.data(), t, sizeof(double) * nsys, cudaMemcpyDeviceToHost));
+  NBG_CUDA(cudaMemcpy(ph.data(), pair, ap, cudaMemcpyDeviceToHost));
+  double *c_t, *c_x, *c_v, *c_xe, *c_ve, *c_J, *c_E, *c_dq, *c_tt, *c_dq0, *c_del;
+  long long* c_cnt;
+  int rc;
+#define GETT(ptr, nm, cnt) if ((rc = ctx->get(nm, (size_t)(cnt), &ptr))) return rc
+  GETT(c_t, "a_t", nsys); GETT(c_x, "a_x", ax); GETT(c_v, "a_v", ax); GETT(c_xe, "a_xe", ax); GETT(c_ve, "a_ve", ax);
+  GETT(c_J, "a_J", aJ); GETT(c_E, "a_E", aJ); GETT(c_dq, "a_dq", adq); GETT(c_tt, "a_tt", att);
+  GETT(c_dq0, "a_dq0", adq0); GETT(c_del, "a_del", adq0); GETT(c_cnt, "a_cnt", am);
+#undef GETT
+  auto reset = [&]() -> int {
+    NBG_CUDA(cudaMemcpyAsync(c_t, t, sizeof(double) * nsys, cudaMemcpyDeviceToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(c_x, x, sizeof(double) * ax, cudaMemcpyDeviceToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(c_v, v, sizeof(double) * ax, cudaMemcpyDeviceToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(c_xe, xerror, sizeof(double) * ax, cudaMemcpyDeviceToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(c_ve, verror, sizeof(double) * ax, cudaMemcpyDeviceToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(c_J, jac_step, sizeof(double) * aJ, cudaMemcpyDeviceToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(c_E, jac_error, sizeof(double) * aJ, cudaMemcpyDeviceToDevice, st));
+    NBG_CUDA(cudaMemcpyAsync(c_dq, dqdt, sizeof(double) * adq, cudaMemcpyDeviceToDevice, st));
+    NBG_CUDA(cudaMemsetAsync(c_cnt, 0, sizeof(long long) * am, st));
+    NBG_CUDA(cudaMemsetAsync(c_tt, 0, sizeof(double) * att, st));
+    NBG_CUDA(cudaMemsetAsync(c_dq0, 0, sizeof(double) * adq0, st));
+    NBG_CUDA(cudaMemsetAsync(c_del, 0, sizeof(double) * adq0, st));
+    return NBG_OK;
+  };
+  struct Cand { int chunk, team, spw; };
+  std::vector<Cand> cands;
+  for (int chunk : {32, 64, 128})
+    for (int team : {0, 1}) {
+      if (team && !any_team) continue;
+      for (int spw : {0, 16}) {
+        if (team && spw) continue;  // explicit lanes per warp select the one-lane producer
+        cands.push_back({chunk, team, spw});
+      }
+    }
+  const int save_chunk = ctx->chunk_steps, save_team = ctx->orbit_team, save_spw = ctx->orbit_spw;
+  const int save_prof = ctx->profile;
+  ctx->profile = 0;
+  int best = -1, nrep = 0;
+  double best_ms = 1e300;
+  std::vector<double> cand_ms;
+  for (size_t q = 0; q <= cands.size(); q++) {
+    const Cand& cd = cands[q == 0 ? 0 : q - 1];  // the first candidate runs twice: the first run allocates
+    ctx->chunk_steps = cd.chunk;
+    ctx->orbit_team = cd.team;
+    ctx->orbit_spw = cd.spw;
+    double tms[2] = {0.0, 0.0};
+    for (int r = 0; r < 2 && !rc; r++) {
+      if ((rc = reset())) break;
+      rc = run_batch(ctx, nsys, r ? td2.data() : td1.data(), th.data(), ph.data(), c_t, c_x, c_v, m, c_xe, c_ve, c_J,
+                     c_E, c_dq, jac_init, c_tt, c_dq0, c_del, c_cnt, nullptr);
+      tms[r] = ctx->last_total_ms;
+    }
+    if (rc) break;
+    if (q == 0) continue;
+    const double T1 = std::min<long long>(longest, trial_steps), T2 = std::min<long long>(longest, 2LL * trial_steps);
+    const double slope = (T2 > T1) ? (tms[1] - tms[0]) / (T2 - T1) : 0.0;
+    const double ms = (T2 > T1) ? tms[0] + std::max(0.0, slope) * ((double)longest - T1) : tms[1];
+    if (report && nrep < report_len) {
+      report[nrep].chunk_steps = cd.chunk;
+      report[nrep].orbit_team = cd.team;
+      report[nrep].orbit_lanes = cd.spw;
+      report[nrep].pad = 0;
+      report[nrep].ms = ms;
+      report[nrep].system_steps_per_s = (double)steps / (ms * 1e-3);
+    }
+    nrep++;
+    cand_ms.push_back(ms);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = (int)q - 1;
+    }
+  }
+  ctx->profile = save_prof;
+  // near-ties (within 2 %, below the trials' noise) go to the longer chunk:
+  // fewer launches and event waits per pass
+  if (!rc && best >= 0) {
+    int pick = best;
+    for (int q = 0; q < (int)cand_ms.size(); q++)
+      if (cand_ms[q] <= 1.02 * best_ms && cands[q].chunk > cands[pick].chunk) pick = q;
+    best = pick;
+  }
+  if (rc || best < 0) {
+    ctx->chunk_steps = save_chunk;
+    ctx->orbit_team = save_team;
+    ctx->orbit_spw = save_spw;
+    return rc ? rc : set_error(NBG_EINVAL, "autotune: no candidate ran");
+  }
+  ctx->chunk_steps = cands[best].chunk;
+  ctx->orbit_team = cands[best].team;
+  ctx->orbit_spw = cands[best].spw;
+  if (nreport) *nreport = std::min(nrep, report_len);
+  return NBG_OK;
+}
+
 int nbg_batch_integrate_transits_noalloc(nbg_context* ctx, int nsys, const nbg_system_desc* desc, double* t,
                                          double* x, double* v, const double* m, double* xerror, double* verror,
                                          double* jac_step, double* jac_error, double* dqdt, const uint8_t* pair,

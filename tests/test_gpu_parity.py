@@ -385,3 +385,33 @@ def test_cartesian_output_trajectory(n):
         colmax = np.max(np.abs(so.jac_step), axis=0, keepdims=True)
         assert np.all(np.abs(o.jac_step[i] - so.jac_step) <= 1e-9 * (np.abs(so.jac_step) + 1e-4 * colmax)), i
         O.integrate_nsteps(so, h, 1)
+
+
+def test_autotuner_leaves_inputs_and_results_unchanged():
+    """nbg_autotune_device times candidates on copies: the caller's device arrays are untouched, and the
+    integration after tuning is bitwise the one with the default mapping."""
+    import torch
+    els, hs, tms = W.batch_uneven(40, seed=99, nmin=2, nmax=7)
+    specs = [(el, h, min(tm, 90 * h), True) for el, h, tm in zip(els, hs, tms)]
+    states, timings, hs, tms, grads = _batch_inputs(specs)
+
+    def batch():
+        b = nbg.Batch([s.n for s in states], 0, hs, tms, [t.ntt for t in timings], grads)
+        for q in range(len(states)):
+            b.set_system(q, states[q], timings[q])
+        return b
+
+    b0 = batch()
+    b0.run()
+    b = batch()
+    dev = {k: torch.from_numpy(a.copy()).cuda() for k, a in b.arrays.items()}
+    before = {k: t.clone() for k, t in dev.items()}
+    ctx = nbg.Context(0)
+    res = b.autotune_device(dev, ctx, trial_steps=40)
+    assert len(res) >= 6 and all(r["ms"] > 0 for r in res)
+    for k in dev:
+        assert torch.equal(dev[k], before[k]), k
+    b.run_device(dev, ctx)
+    for k in ("x", "v", "tt", "count", "jac_step", "dtdq0", "dtdelements"):
+        assert np.array_equal(dev[k].cpu().numpy(), b0.arrays[k]), k
+    ctx.close()
