@@ -398,7 +398,9 @@ int nbg_set_orbit_lanes(nbg_context* ctx, int systems_per_warp);
  * the reference. */
 int nbg_set_orbit_team(nbg_context* ctx, int mode);
 
-/* Record an event pair around every orbit / Jacobian launch (off by default). */
+/* Record an event pair around kernel launches (0: off, the default; 1: every
+ * orbit-producer, transit, operator and Jacobian launch; 2: the Jacobian
+ * consumer's launches only, which perturbs the pipeline least). */
 int nbg_set_profiling(nbg_context* ctx, int on);
 
 /* Launch counts of the last call, per kernel kind. */

@@ -352,7 +352,7 @@ class Batch:
 
     def autotune_device(self, dev_arrays, ctx=None, trial_steps=256):
         """nbg_autotune_device on device buffers: picks the fastest mapping for this batch on ctx and
-        returns the candidates' trial timings (a list of dicts, the chosen one first)."""
+        returns the candidates' predicted times (a list of dicts, the chosen one first)."""
         import ctypes
         ctx = ctx or default_context()
         L = _lib.load()
@@ -366,7 +366,7 @@ class Batch:
             rep, 32, ctypes.byref(nrep)))
         out = [{k: getattr(rep[q], k) for k, _ in _lib.TuningResult._fields_ if k != "pad"}
                for q in range(nrep.value)]
-        return sorted(out, key=lambda r: r["ms"])
+        return out[:1] + sorted(out[1:], key=lambda r: r["ms"])
 
     def run_device_noalloc(self, dev_arrays, ctx=None):
         """nbg_batch_integrate_transits_noalloc on device buffers: the same call

@@ -219,7 +219,8 @@ class Context:
         check(load().nbg_set_orbit_team(self._h, int(mode)))
 
     def set_profiling(self, on=True):
-        check(load().nbg_set_profiling(self._h, int(bool(on))))
+        """0 / False: off; 1 / True: every kernel kind; 2: the Jacobian consumer only."""
+        check(load().nbg_set_profiling(self._h, int(on)))
 
     def last_kernel_stats(self):
         a, b = ctypes.c_int64(), ctypes.c_int64()

@@ -600,7 +600,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
   std::vector<std::pair<int, size_t>> prof;  // (kind, first event index)
   size_t nev = 0;
   auto timed = [&](int kind, auto&& launch) -> int {
-    if (!ctx->profile) return launch();
+    if (!ctx->profile || (ctx->profile == 2 && kind != 1)) return launch();
     cudaEvent_t a, b;
     int r;
     if ((r = ctx->event(nev, &a)) || (r = ctx->event(nev + 1, &b))) return r;
@@ -614,7 +614,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
   // the same on another stream: the event pair brackets the launch on the
   // stream it is launched on
   auto timed_on = [&](cudaStream_t s2, int kind, auto&& launch) -> int {
-    if (!ctx->profile) return launch();
+    if (!ctx->profile || (ctx->profile == 2 && kind != 1)) return launch();
     cudaEvent_t a, b;
     int r;
     if ((r = ctx->event(nev, &a)) || (r = ctx->event(nev + 1, &b))) return r;
@@ -1181,7 +1181,8 @@ int nbg_set_orbit_team(nbg_context* ctx, int mode) {
 
 int nbg_set_profiling(nbg_context* ctx, int on) {
   if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
-  ctx->profile = on ? 1 : 0;
+  if (on < 0 || on > 2) return set_error(NBG_EINVAL, "profiling level %d not in 0..2", on);
+  ctx->profile = on;
   return NBG_OK;
 }
 
@@ -1671,14 +1672,8 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
     }
   }
   ctx->profile = save_prof;
-  // near-ties (within 2 %, below the trials' noise) go to the longer chunk:
-  // fewer launches and event waits per pass
-  if (!rc && best >= 0) {
-    int pick = best;
-    for (int q = 0; q < (int)cand_ms.size(); q++)
-      if (cand_ms[q] <= 1.02 * best_ms && cands[q].chunk > cands[pick].chunk) pick = q;
-    best = pick;
-  }
+  // the chosen candidate first in the report
+  if (!rc && best > 0 && report && best < std::min(nrep, report_len)) std::swap(report[0], report[best]);
   if (rc || best < 0) {
     ctx->chunk_steps = save_chunk;
     ctx->orbit_team = save_team;
