@@ -515,9 +515,11 @@ def main():
                                       else {0: "off", 1: "on"}[tuning[0]["orbit_team"]]),
                        "autotuner": None if tuning is None else {
                            "trial_steps_per_system": args.tune_steps,
-                           "chosen": {k: tuning[0][k] for k in ("chunk_steps", "orbit_team", "orbit_lanes")},
+                           "chosen": {k: tuning[0][k] for k in ("chunk_steps", "orbit_team", "producer_warps",
+                                                                "producer_smem_kb")},
                            "candidates": [{k: (round(r[k], 2) if k == "ms" else r[k])
-                                           for k in ("chunk_steps", "orbit_team", "orbit_lanes", "ms")}
+                                           for k in ("chunk_steps", "orbit_team", "producer_warps",
+                                                     "producer_smem_kb", "ms")}
                                           for r in tuning]},
                        "streams": 1 if args.serial else 3},
             "e2e": {"value": e2e_val, "unit": "system-steps/s", "h2d_bytes_per_step": int(h2d),

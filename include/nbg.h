@@ -366,8 +366,10 @@ int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double
  * integrations of this batch -- every system's first min(nsteps, T) steps
  * for T = trial_steps and 2 trial_steps, on device copies (the caller's
  * arrays are not modified) -- for each candidate mapping: steps per chunk
- * {32, 64, 128} x orbit producer form {one lane per system, team of lanes} x
- * producer systems per warp {automatic, 16}.  The two trial times extrapolate
+ * {64, 128} x orbit producer form {one lane per system, team of lanes} x
+ * producer block layout {one warp; four warps holding 200 KB of shared
+ * memory, operator and search blocks 32 KB} (nbg_set_producer_layout).  The
+ * two trial times extrapolate
  * the chunk loop's time to the batch's longest system (pipeline fill and
  * drain plus a steady cost per step); the fastest candidate is kept on the
  * context (as nbg_set_tuning / nbg_set_orbit_team / nbg_set_orbit_lanes
@@ -376,7 +378,8 @@ int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double
  * their number.  Results of later calls do not depend on the choice.
  */
 typedef struct {
-  int32_t chunk_steps, orbit_team, orbit_lanes, pad;
+  int32_t chunk_steps, orbit_team, orbit_lanes;
+  int32_t producer_warps, producer_smem_kb, pad;
   double ms;                 /* predicted chunk-loop time of the full batch   */
   double system_steps_per_s; /* the batch's system-steps / that time          */
 } nbg_tuning_result;
@@ -397,6 +400,16 @@ int nbg_set_orbit_lanes(nbg_context* ctx, int systems_per_warp);
  * and so gives bitwise the same results.  A tuning knob; no counterpart in
  * the reference. */
 int nbg_set_orbit_team(nbg_context* ctx, int mode);
+
+/* Block layout of the orbit producer (a tuning knob; no counterpart in the
+ * reference; results do not depend on it): warps_per_block (1..4)
+ * independent producer warps per block, each block holding smem_kb KB of
+ * shared memory (0..220), and guard_kb KB (0..100) requested by every
+ * operator-record and transit-search block.  Blocks cannot share an SM when
+ * their shared memory exceeds the SM's 227 KB, so smem_kb = 200 with
+ * guard_kb = 32 keeps the throughput kernels off the SMs that run the
+ * latency-bound producer.  Default 1, 0, 0. */
+int nbg_set_producer_layout(nbg_context* ctx, int warps_per_block, int smem_kb, int guard_kb);
 
 /* Record an event pair around kernel launches (0: off, the default; 1: every
  * orbit-producer, transit, operator and Jacobian launch; 2: the Jacobian

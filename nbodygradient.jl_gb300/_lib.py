@@ -32,6 +32,7 @@ EXPORTS = (
     "nbg_integrate_transits", "nbg_batch_integrate_transits", "nbg_batch_integrate_transits_device",
     "nbg_set_tuning", "nbg_last_timing", "nbg_last_launch_count", "nbg_fp64_peak",
     "nbg_set_profiling", "nbg_last_kernel_stats", "nbg_set_orbit_lanes", "nbg_set_orbit_team",
+    "nbg_set_producer_layout",
     "nbg_batch_integrate_transits_noalloc",
     "nbg_integrate", "nbg_integrate_steps", "nbg_batch_integrate",
     "nbg_integrate_transit_parameters", "nbg_batch_integrate_transit_parameters",
@@ -60,7 +61,8 @@ class DeviceInfo(ctypes.Structure):
 
 class TuningResult(ctypes.Structure):
     _fields_ = [("chunk_steps", ctypes.c_int32), ("orbit_team", ctypes.c_int32), ("orbit_lanes", ctypes.c_int32),
-                ("pad", ctypes.c_int32), ("ms", ctypes.c_double), ("system_steps_per_s", ctypes.c_double)]
+                ("producer_warps", ctypes.c_int32), ("producer_smem_kb", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("ms", ctypes.c_double), ("system_steps_per_s", ctypes.c_double)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -141,6 +143,7 @@ def load(build_if_missing=True):
     L.nbg_set_profiling.argtypes = [_VP, ctypes.c_int]
     L.nbg_set_orbit_lanes.argtypes = [_VP, ctypes.c_int]
     L.nbg_set_orbit_team.argtypes = [_VP, ctypes.c_int]
+    L.nbg_set_producer_layout.argtypes = [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.nbg_last_kernel_stats.argtypes = [_VP, _I64, _I64]
     L.nbg_server_start.argtypes = [ctypes.c_int, ctypes.POINTER(ServerConfig), ctypes.POINTER(_VP)]
     L.nbg_server_enqueue.argtypes = [_VP, ctypes.POINTER(SystemDesc), ctypes.c_double, _D, _D, _D, _D, _D, _D, _D,
@@ -217,6 +220,9 @@ class Context:
     def set_orbit_team(self, mode=-1):
         """-1 automatic, 0 one lane per system, 1 a team of lanes per system."""
         check(load().nbg_set_orbit_team(self._h, int(mode)))
+
+    def set_producer_layout(self, warps_per_block=1, smem_kb=0, guard_kb=0):
+        check(load().nbg_set_producer_layout(self._h, int(warps_per_block), int(smem_kb), int(guard_kb)))
 
     def set_profiling(self, on=True):
         """0 / False: off; 1 / True: every kernel kind; 2: the Jacobian consumer only."""

@@ -228,6 +228,7 @@ struct nbg_context {
   int overlap = 1;  // orbit producer on its own stream, one chunk ahead of the rest
   int orbit_spw = 0;  // 0: automatic
   int orbit_team = -1;  // -1: automatic (teams for N >= 5), 0: one lane per system, 1: teams for every N
+  int prod_warps = 1, prod_smem_kb = 0, guard_smem_kb = 0;  // orbit producer block layout
   int sm_count = 0;
   double last_total_ms = 0, last_orbit_ms = 0, last_jac_ms = 0, last_transit_ms = 0, last_ops_ms = 0;
   long long last_launches = 0, last_orbit_launches = 0, last_jac_launches = 0;
@@ -455,6 +456,9 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     // the most FP64 issue slots to the kernels running beside the producer.
     // Without overlap a small batch is spread over about two warps per SM.
     g.team = use_team(ctx->orbit_team, N, gp.kick) && ctx->orbit_spw == 0;
+    g.pwarps = ctx->prod_warps;
+    g.prod_smem = ctx->prod_smem_kb * 1024;
+    g.guard_smem = ctx->guard_smem_kb * 1024;
     if (ctx->orbit_spw > 0) {
       g.spw = ctx->orbit_spw;
     } else if (ctx->overlap) {
@@ -1172,6 +1176,18 @@ int nbg_set_orbit_lanes(nbg_context* ctx, int systems_per_warp) {
   return NBG_OK;
 }
 
+int nbg_set_producer_layout(nbg_context* ctx, int warps_per_block, int smem_kb, int guard_kb) {
+  if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
+  if (warps_per_block < 1 || warps_per_block > PROD_MAX_WARPS)
+    return set_error(NBG_EINVAL, "warps_per_block = %d not in 1..%d", warps_per_block, PROD_MAX_WARPS);
+  if (smem_kb < 0 || smem_kb > 220 || guard_kb < 0 || guard_kb > 100)
+    return set_error(NBG_EINVAL, "smem_kb = %d (0..220), guard_kb = %d (0..100)", smem_kb, guard_kb);
+  ctx->prod_warps = warps_per_block;
+  ctx->prod_smem_kb = smem_kb;
+  ctx->guard_smem_kb = guard_kb;
+  return NBG_OK;
+}
+
 int nbg_set_orbit_team(nbg_context* ctx, int mode) {
   if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
   if (mode < -1 || mode > 1) return set_error(NBG_EINVAL, "mode = %d not in -1..1", mode);
@@ -1623,17 +1639,19 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
     NBG_CUDA(cudaMemsetAsync(c_del, 0, sizeof(double) * adq0, st));
     return NBG_OK;
   };
-  struct Cand { int chunk, team, spw; };
+  struct Cand { int chunk, team, spw, pw, smem, guard; };
   std::vector<Cand> cands;
-  for (int chunk : {32, 64, 128})
+  for (int chunk : {64, 128})
     for (int team : {0, 1}) {
       if (team && !any_team) continue;
-      for (int spw : {0, 16}) {
-        if (team && spw) continue;  // explicit lanes per warp select the one-lane producer
-        cands.push_back({chunk, team, spw});
-      }
+      // producer blocks of one warp anywhere, or of four warps holding their
+      // SM's shared memory so that consumer, operator and search blocks run
+      // on the other SMs
+      cands.push_back({chunk, team, 0, 1, 0, 0});
+      cands.push_back({chunk, team, 0, 4, 200, 32});
     }
   const int save_chunk = ctx->chunk_steps, save_team = ctx->orbit_team, save_spw = ctx->orbit_spw;
+  const int save_pw = ctx->prod_warps, save_sm = ctx->prod_smem_kb, save_gd = ctx->guard_smem_kb;
   const int save_prof = ctx->profile;
   ctx->profile = 0;
   int best = -1, nrep = 0;
@@ -1644,6 +1662,9 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
     ctx->chunk_steps = cd.chunk;
     ctx->orbit_team = cd.team;
     ctx->orbit_spw = cd.spw;
+    ctx->prod_warps = cd.pw;
+    ctx->prod_smem_kb = cd.smem;
+    ctx->guard_smem_kb = cd.guard;
     double tms[2] = {0.0, 0.0};
     for (int r = 0; r < 2 && !rc; r++) {
       if ((rc = reset())) break;
@@ -1660,7 +1681,8 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
       report[nrep].chunk_steps = cd.chunk;
       report[nrep].orbit_team = cd.team;
       report[nrep].orbit_lanes = cd.spw;
-      report[nrep].pad = 0;
+      report[nrep].producer_warps = cd.pw;
+      report[nrep].producer_smem_kb = cd.smem;
       report[nrep].ms = ms;
       report[nrep].system_steps_per_s = (double)steps / (ms * 1e-3);
     }
@@ -1678,11 +1700,17 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
     ctx->chunk_steps = save_chunk;
     ctx->orbit_team = save_team;
     ctx->orbit_spw = save_spw;
+    ctx->prod_warps = save_pw;
+    ctx->prod_smem_kb = save_sm;
+    ctx->guard_smem_kb = save_gd;
     return rc ? rc : set_error(NBG_EINVAL, "autotune: no candidate ran");
   }
   ctx->chunk_steps = cands[best].chunk;
   ctx->orbit_team = cands[best].team;
   ctx->orbit_spw = cands[best].spw;
+  ctx->prod_warps = cands[best].pw;
+  ctx->prod_smem_kb = cands[best].smem;
+  ctx->guard_smem_kb = cands[best].guard;
   if (nreport) *nreport = std::min(nrep, report_len);
   return NBG_OK;
 }

@@ -12,6 +12,8 @@
 // Systems are grouped by (N, grad, kick pattern) so that every warp runs one
 // control-flow path; within a group systems are sorted longest first.
 #pragma once
+#include <algorithm>
+
 #include "../../include/nbg.h"
 #include "nbg_jacobian.cuh"
 #include "nbg_orbit_team.cuh"
@@ -20,9 +22,10 @@ namespace nbg {
 
 // Orbit producer for one chunk of K steps of one group (one lane per system).
 template <int N>
-__global__ void __launch_bounds__(PROD_BS) orbit_chunk_kernel(GroupArgs g, int chunk) {
-  if ((int)threadIdx.x >= g.spw) return;
-  const int s = blockIdx.x * g.spw + threadIdx.x;
+__global__ void __launch_bounds__(PROD_BS * PROD_MAX_WARPS) orbit_chunk_kernel(GroupArgs g, int chunk) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane >= g.spw) return;
+  const int s = (blockIdx.x * (g.pwarps > 0 ? g.pwarps : 1) + warp) * g.spw + lane;
   if (s >= g.S || g.sysidx[s] < 0) return;
   const int S = g.S;
   const long long nst = g.nsteps[s];
@@ -408,15 +411,25 @@ __global__ void seed_gsave_kernel(GroupArgs g) {
   }
 }
 
+// Dynamic shared memory above the default 48 KB must be allowed per kernel.
+template <class K>
+inline void allow_smem(K kernel, int bytes) {
+  if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 template <int N>
 int launch_orbit(const GroupArgs& g, int chunk, cudaStream_t st) {
+  const int W = g.pwarps > 0 ? g.pwarps : 1;
   if (g.team && !g.kick) {
     constexpr int T = PROD_BS / team_lanes(N);
-    orbit_team_kernel<N><<<(g.S + T - 1) / T, PROD_BS, 0, st>>>(g, chunk);
+    const int smem = std::max(team_smem_bytes<N>(W), g.prod_smem);
+    allow_smem(orbit_team_kernel<N>, smem);
+    orbit_team_kernel<N><<<(g.S + W * T - 1) / (W * T), PROD_BS * W, smem, st>>>(g, chunk);
     return 0;
   }
-  int blocks = (g.S + g.spw - 1) / g.spw;
-  orbit_chunk_kernel<N><<<blocks, PROD_BS, 0, st>>>(g, chunk);
+  const int blocks = (g.S + W * g.spw - 1) / (W * g.spw);
+  allow_smem(orbit_chunk_kernel<N>, g.prod_smem);
+  orbit_chunk_kernel<N><<<blocks, PROD_BS * W, g.prod_smem, st>>>(g, chunk);
   return 0;
 }
 
@@ -436,16 +449,20 @@ int launch_jac(const GroupArgs& g, int chunk, cudaStream_t st) {
 
 template <int N>
 int launch_transit(const GroupArgs& g, int chunk, cudaStream_t st) {
-  transit_kernel<N><<<g.tgrid / TRANSIT_BS, TRANSIT_BS, 0, st>>>(g, chunk);
+  allow_smem(transit_kernel<N>, g.guard_smem);
+  transit_kernel<N><<<g.tgrid / TRANSIT_BS, TRANSIT_BS, g.guard_smem, st>>>(g, chunk);
   return 0;
 }
 
 template <int N>
 int launch_operators(const GroupArgs& g, int chunk, cudaStream_t st) {
   long long lanes = (long long)g.K * 2 * g.npk * g.S;
-  if (lanes > 0) operator_pair_kernel<N><<<(unsigned)((lanes + OPS_BS - 1) / OPS_BS), OPS_BS, 0, st>>>(g, chunk);
+  allow_smem(operator_pair_kernel<N>, g.guard_smem);
+  allow_smem(operator_phi_kernel<N>, g.guard_smem);
+  if (lanes > 0)
+    operator_pair_kernel<N><<<(unsigned)((lanes + OPS_BS - 1) / OPS_BS), OPS_BS, g.guard_smem, st>>>(g, chunk);
   lanes = (long long)g.K * g.S;
-  operator_phi_kernel<N><<<(unsigned)((lanes + OPS_BS - 1) / OPS_BS), OPS_BS, 0, st>>>(g, chunk);
+  operator_phi_kernel<N><<<(unsigned)((lanes + OPS_BS - 1) / OPS_BS), OPS_BS, g.guard_smem, st>>>(g, chunk);
   return 0;
 }
 

@@ -21,7 +21,8 @@ __host__ __device__ inline int step_record_size(int N, int npk, bool kick) {
   return (kick ? 2 * op_size(N) : 0) + 2 * npk * PREC + op_size(N);
 }
 
-constexpr int PROD_BS = 32;     // orbit producer: one warp per block, spread over SMs
+constexpr int PROD_BS = 32;     // orbit producer: threads per warp-sized unit of work
+constexpr int PROD_MAX_WARPS = 4;  // orbit producer: up to 4 independent warps per block
 constexpr int CONS_BS = 128;    // Jacobian consumer: four warps per block
 constexpr int TRANSIT_BS = 32;  // transit searches: one warp per block
 constexpr int OPS_BS = 128;     // operator kernels
@@ -43,6 +44,12 @@ struct GroupArgs {
   int N, S, nsys, grad, K, R, npk;
   int spw;   // orbit producer: systems per warp (lanes >= spw idle)
   int team;  // orbit producer: 1 = a team of lanes per system (orbit_team_kernel), 0 = one lane
+  // Block layout of the orbit producer: pwarps independent warps per block
+  // (0 or 1: one) and prod_smem bytes of dynamic shared memory per block (at
+  // least what the team form needs).  A large allocation keeps the
+  // shared-memory-hungry consumer blocks, and the operator / search blocks
+  // that ask for guard_smem bytes, off the SMs that run producer blocks.
+  int pwarps, prod_smem, guard_smem;
   unsigned long long kick;
   // per-system state, structure of arrays: element e of system s at [e * S + s]
   double *x, *v, *xe, *ve, *m, *dqdt, *gsave;

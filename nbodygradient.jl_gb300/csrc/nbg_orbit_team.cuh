@@ -126,22 +126,32 @@ __device__ __forceinline__ void team_step(Sys<N>& s, double* a, Work<N>& w, int 
   __syncwarp();
 }
 
-// Orbit producer, team form: L lanes per system, T = 32 / L systems per warp
-// (lanes beyond T * L idle).  Same inputs, outputs and arithmetic as
-// orbit_chunk_kernel<N> for groups without kick pairs.
+// Dynamic shared memory the team producer needs for W warps per block:
+// per team a Sys<N>, 3N accelerations, N g values and N transit counts.
 template <int N>
-__global__ void __launch_bounds__(PROD_BS) orbit_team_kernel(GroupArgs g, int chunk) {
+__host__ __device__ constexpr int team_smem_bytes(int W) {
+  return W * (PROD_BS / team_lanes(N)) * (int)(sizeof(Sys<N>) + (3 * N + N) * sizeof(double) + N * sizeof(long long));
+}
+
+// Orbit producer, team form: L lanes per system, T = 32 / L systems per warp
+// (lanes beyond T * L idle), pwarps independent warps per block.  Same
+// inputs, outputs and arithmetic as orbit_chunk_kernel<N> for groups
+// without kick pairs.
+template <int N>
+__global__ void __launch_bounds__(PROD_BS * PROD_MAX_WARPS) orbit_team_kernel(GroupArgs g, int chunk) {
   constexpr int L = team_lanes(N);
   constexpr int T = PROD_BS / L;
-  __shared__ Sys<N> sys[T];
-  __shared__ double acc[T][3 * N];
-  __shared__ double gsv[T][N];
-  __shared__ long long cnt[T][N];
-  const int lane = threadIdx.x;
+  const int W = g.pwarps > 0 ? g.pwarps : 1;
+  extern __shared__ double team_smem[];
+  Sys<N>* sys = reinterpret_cast<Sys<N>*>(team_smem);
+  double(*acc)[3 * N] = reinterpret_cast<double(*)[3 * N]>(sys + W * T);
+  double(*gsv)[N] = reinterpret_cast<double(*)[N]>(acc + W * T);
+  long long(*cnt)[N] = reinterpret_cast<long long(*)[N]>(gsv + W * T);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int team = lane / L, t = lane % L;
   const bool in_team = team < T;
-  const int tm = in_team ? team : 0;  // idle lanes alias team 0 but never write
-  const int s = blockIdx.x * T + tm;
+  const int tm = warp * T + (in_team ? team : 0);  // idle lanes alias their warp's team 0 but never write
+  const int s = blockIdx.x * W * T + tm;
   const int S = g.S;
   bool valid = in_team && s < S && g.sysidx[s] >= 0;
   const long long nst = valid ? g.nsteps[s] : 0;

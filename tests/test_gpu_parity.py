@@ -210,17 +210,19 @@ def test_batch_matches_oracle():
 @pytest.mark.parametrize("grad", [True, False])
 def test_team_producer_is_bitwise_the_one_lane_producer(grad):
     """The team form of the orbit producer (level-parallel sweeps) against the
-    one-lane form, for every body count: bitwise the same x, v, jac_step,
-    transit times and derivatives."""
+    one-lane form, and both in multi-warp blocks holding their SM's shared
+    memory, for every body count: bitwise the same x, v, jac_step, transit
+    times and derivatives."""
     specs = []
     for n in range(2, 11):
         els, hs, tms = W.batch_uneven(3, seed=40 + n, nmin=n, nmax=n)
         specs += [(el, h, 90 * h, grad) for el, h in zip(els, hs)]
     states, timings, hs, tms, grads = _batch_inputs(specs)
     out = []
-    for mode in (0, 1):
+    for mode, layout in ((0, (1, 0, 0)), (1, (1, 0, 0)), (0, (4, 200, 32)), (1, (4, 200, 32)), (1, (3, 0, 0))):
         ctx = nbg.Context(0)
         ctx.set_orbit_team(mode)
+        ctx.set_producer_layout(*layout)
         b = nbg.Batch([s.n for s in states], 0, hs, tms, [t.ntt for t in timings], grads)
         for q in range(len(states)):
             b.set_system(q, states[q], timings[q])
@@ -228,8 +230,10 @@ def test_team_producer_is_bitwise_the_one_lane_producer(grad):
         out.append(b)
         ctx.close()
     assert sum(int(c) for c in out[0].arrays["count"]) > 0
-    for k in ("x", "v", "xerror", "verror", "tt", "count", "jac_step", "jac_error", "dtdq0", "dtdelements", "dqdt"):
-        assert np.array_equal(out[0].arrays[k], out[1].arrays[k]), k
+    for b in out[1:]:
+        for k in ("x", "v", "xerror", "verror", "tt", "count", "jac_step", "jac_error", "dtdq0", "dtdelements",
+                  "dqdt"):
+            assert np.array_equal(out[0].arrays[k], b.arrays[k]), k
 
 
 @pytest.mark.parametrize("n", [3, 5, 8])
