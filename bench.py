@@ -349,7 +349,8 @@ def main():
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--serial", action="store_true", help="one stream: no producer/consumer overlap")
     ap.add_argument("--kernel-timing", default="timed", choices=["timed", "separate"],
-                    help="CUDA-event pairs around each kernel inside the timed steps, or in one extra pass")
+                    help="consumer duration from a CUDA-event pair around one launch per timed step, or from "
+                         "event pairs around every launch in one extra pass")
     ap.add_argument("--spw", type=int, default=0, help="orbit producer systems per warp (0 = automatic)")
     ap.add_argument("--orbit-team", type=int, default=-1,
                     help="orbit producer form: -1 automatic, 0 one lane per system, 1 a team per system")
@@ -429,9 +430,11 @@ def main():
     launches = 0
     # per-kernel CUDA-event pairs on each kernel's own stream, summed over the
     # timed steps: the roofline's kernel durations come from the timed region
-    # event pairs around the Jacobian consumer's launches only (the roofline
-    # kernel): timing every kernel kind perturbs the pipeline by a few percent
-    ctx.set_profiling(2 if args.kernel_timing == "timed" else 0)
+    # one event pair per timed step, around the Jacobian consumer's launch of
+    # the middle chunk (the roofline kernel's duration, measured inside the
+    # timed region): an event pair around every consumer launch slows the
+    # overlapped streams by 8-10 % (measured), one pair per step does not
+    ctx.set_profiling(3 if args.kernel_timing == "timed" else 0)
     kt = np.zeros(4)
     kn = np.zeros(2, dtype=np.int64)
     torch.cuda.synchronize()
@@ -528,7 +531,12 @@ def main():
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                          "kernel": "jacobian_chunk_kernel", "peak_source": "measured live (nbg_fp64_peak, DFMA)",
-                         "launches": n_jac, "kernel_ms": jac_ms, "orbit_ms": orbit_ms, "transit_ms": transit_ms,
+                         "launches": n_jac, "kernel_ms": jac_ms,
+                         "kernel_ms_source": ("CUDA-event pair around one consumer launch (the middle chunk) per "
+                                              "timed step, on its stream, scaled to the step's launches"
+                                              if args.kernel_timing == "timed" else
+                                              "CUDA-event pairs around every consumer launch of one extra pass"),
+                         "orbit_ms": orbit_ms, "transit_ms": transit_ms,
                          "loop_ms": total_ms},
             "clocks": clocks,
         }

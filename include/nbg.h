@@ -413,7 +413,10 @@ int nbg_set_producer_layout(nbg_context* ctx, int warps_per_block, int smem_kb, 
 
 /* Record an event pair around kernel launches (0: off, the default; 1: every
  * orbit-producer, transit, operator and Jacobian launch; 2: the Jacobian
- * consumer's launches only, which perturbs the pipeline least). */
+ * consumer's launches; 3: one consumer launch per group and call, its
+ * middle chunk, with nbg_last_timing's jacobian_ms scaled to all the
+ * consumer launches -- event pairs delay the overlapped streams, and one
+ * pair per call perturbs them least). */
 int nbg_set_profiling(nbg_context* ctx, int on);
 
 /* Launch counts of the last call, per kernel kind. */

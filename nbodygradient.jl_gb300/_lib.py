@@ -225,7 +225,7 @@ class Context:
         check(load().nbg_set_producer_layout(self._h, int(warps_per_block), int(smem_kb), int(guard_kb)))
 
     def set_profiling(self, on=True):
-        """0 / False: off; 1 / True: every kernel kind; 2: the Jacobian consumer only."""
+        """0 / False: off; 1 / True: every kernel kind; 2: the Jacobian consumer; 3: one sampled consumer launch."""
         check(load().nbg_set_profiling(self._h, int(on)))
 
     def last_kernel_stats(self):

@@ -600,11 +600,18 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     }
     return NBG_OK;
   };
-  // profiling: an event pair around every orbit / Jacobian launch
+  // profiling: an event pair around every launch (level 1), every Jacobian
+  // consumer launch (2), or one consumer launch per group -- its middle
+  // chunk (3)
   std::vector<std::pair<int, size_t>> prof;  // (kind, first event index)
   size_t nev = 0;
+  bool sample_now = false;  // level 3: this launch is the group's sampled one
+  long long sampled = 0;
+  auto skip = [&](int kind) {
+    return !ctx->profile || (ctx->profile >= 2 && kind != 1) || (ctx->profile == 3 && !sample_now);
+  };
   auto timed = [&](int kind, auto&& launch) -> int {
-    if (!ctx->profile || (ctx->profile == 2 && kind != 1)) return launch();
+    if (skip(kind)) return launch();
     cudaEvent_t a, b;
     int r;
     if ((r = ctx->event(nev, &a)) || (r = ctx->event(nev + 1, &b))) return r;
@@ -618,7 +625,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
   // the same on another stream: the event pair brackets the launch on the
   // stream it is launched on
   auto timed_on = [&](cudaStream_t s2, int kind, auto&& launch) -> int {
-    if (!ctx->profile || (ctx->profile == 2 && kind != 1)) return launch();
+    if (skip(kind)) return launch();
     cudaEvent_t a, b;
     int r;
     if ((r = ctx->event(nev, &a)) || (r = ctx->event(nev + 1, &b))) return r;
@@ -643,6 +650,8 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
         ctx->last_orbit_launches++;
         if (g.grad) {
           if ((rc = timed(3, [&] { return kOps[g.N](g, (int)c, st); }))) return rc;
+          sample_now = (c == ((gmaxsteps[q] + K - 1) / K) / 2);
+          sampled += (ctx->profile == 3 && sample_now) ? 1 : 0;
           if ((rc = timed(1, [&] { return kJac[g.N](g, (int)c, st); }))) return rc;
           ctx->last_launches += 3;
           ctx->last_jac_launches++;
@@ -694,6 +703,8 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
         if (g.grad) {
           if ((rc = timed_on(sw, 3, [&] { return kOps[g.N](g, (int)c, sw); }))) return rc;
           NBG_CUDA(cudaStreamWaitEvent(sw, ev_tr, 0));
+          sample_now = (c == ((gmaxsteps[q] + K - 1) / K) / 2);
+          sampled += (ctx->profile == 3 && sample_now) ? 1 : 0;
           if ((rc = timed_on(sw, 1, [&] { return kJac[g.N](g, (int)c, sw); }))) return rc;
           ctx->last_launches += 3;
           ctx->last_jac_launches++;
@@ -752,6 +763,8 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     (pr.first == 1 ? ctx->last_jac_ms : pr.first == 2 ? ctx->last_transit_ms
                                       : pr.first == 3 ? ctx->last_ops_ms : ctx->last_orbit_ms) += e;
   }
+  // level 3: the sampled launches stand for all of them
+  if (ctx->profile == 3 && sampled > 0) ctx->last_jac_ms *= (double)ctx->last_jac_launches / (double)sampled;
   if (status_host) {
     std::fill(status_host, status_host + nsys, 0u);
     for (auto& g : gargs) {
@@ -1197,7 +1210,7 @@ int nbg_set_orbit_team(nbg_context* ctx, int mode) {
 
 int nbg_set_profiling(nbg_context* ctx, int on) {
   if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
-  if (on < 0 || on > 2) return set_error(NBG_EINVAL, "profiling level %d not in 0..2", on);
+  if (on < 0 || on > 3) return set_error(NBG_EINVAL, "profiling level %d not in 0..3", on);
   ctx->profile = on;
   return NBG_OK;
 }
