@@ -437,12 +437,8 @@ template <int N>
 int launch_jac(const GroupArgs& g, int chunk, cudaStream_t st) {
   long long threads = (long long)g.S * 7 * N;
   int blocks = (int)((threads + CONS_BS - 1) / CONS_BS);
-  size_t smem = (size_t)2 * 6 * N * CONS_BS * sizeof(double);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(jacobian_chunk_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr_set = true;
-  }
+  const int smem = 2 * 6 * N * CONS_BS * (int)sizeof(double);
+  allow_smem(jacobian_chunk_kernel<N>, smem);  // per call: the attribute belongs to the current device
   jacobian_chunk_kernel<N><<<blocks, CONS_BS, smem, st>>>(g, chunk);
   return 0;
 }
