@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(PROD_BS * PROD_MAX_WARPS) orbit_chunk_kernel(G
   const int S = g.S;
   const long long nst = g.nsteps[s];
   const long long k0 = chunk_first_step(g, chunk, s);
-  if (k0 >= nst) return;
+  if (k0 >= nst || k0 < 0) return;  // done, or admitted for a later chunk
   Sys<N> st;
   Work<N> w;
   for (int q = 0; q < 3 * N; q++) {
@@ -259,7 +259,8 @@ __global__ void __launch_bounds__(OPS_BS) operator_pair_kernel(GroupArgs g, int 
   const long long rest = L / S;
   const int slot = (int)(rest % np2), kk = (int)(rest / np2);
   if (g.sysidx[s] < 0) return;
-  if (chunk_first_step(g, chunk, s) + kk >= g.nsteps[s]) return;
+  const long long istep = chunk_first_step(g, chunk, s) + kk;
+  if (istep >= g.nsteps[s] || istep < 0) return;
   const uint64_t kick = g.kick;
   Rec cap{g.pcap + (size_t)kk * np2 * PCAP * S + s, S};
   Rec rec{g.steprec + (size_t)kk * g.R * S + s, S};
@@ -289,7 +290,7 @@ __global__ void __launch_bounds__(OPS_BS) operator_phi_kernel(GroupArgs g, int c
   const int s = (int)(L % S), kk = (int)(L / S);
   if (g.sysidx[s] < 0) return;
   const long long istep = chunk_first_step(g, chunk, s) + kk;
-  if (istep >= g.nsteps[s]) return;
+  if (istep >= g.nsteps[s] || istep < 0) return;
   const uint64_t kick = g.kick;
   const double h = step_length(g, s, istep, g.nsteps[s], g.h[s]);
   Rec xs{g.xsnap + (size_t)kk * snap_count(kick != 0) * 3 * N * S + s, S};
@@ -324,7 +325,7 @@ __global__ void __launch_bounds__(CONS_BS) jacobian_chunk_kernel(GroupArgs g, in
   const int S = g.S;
   const long long nst = g.nsteps[s];
   const long long k0 = chunk_first_step(g, chunk, s);
-  if (k0 >= nst) return;
+  if (k0 >= nst || k0 < 0) return;  // done, or admitted for a later chunk
   double* J = smem + threadIdx.x;
   double* E = smem + R6 * CONS_BS + threadIdx.x;
   const double* Jg = g.Jint + (size_t)s * R6 * M + c;

@@ -99,7 +99,9 @@ __device__ __forceinline__ double step_length(const GroupArgs& g, int s, long lo
   return (g.hlast && istep == nst - 1) ? g.hlast[s] : h;
 }
 
-// Index of the first step of chunk `chunk` for the system in slot s.
+// Index of the first step of chunk `chunk` for the system in slot s (negative
+// while the slot's system is admitted for a later chunk: the request server
+// writes a slot's settings while the previous chunk's kernels may still run).
 __device__ __forceinline__ long long chunk_first_step(const GroupArgs& g, int chunk, int s) {
   return (long long)chunk * g.K - (g.kbase ? g.kbase[s] : 0);
 }

@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(PROD_BS * PROD_MAX_WARPS) orbit_team_kernel(Gr
   bool valid = in_team && s < S && g.sysidx[s] >= 0;
   const long long nst = valid ? g.nsteps[s] : 0;
   const long long k0 = valid ? chunk_first_step(g, chunk, s) : 0;
-  if (k0 >= nst) valid = false;
+  if (k0 >= nst || k0 < 0) valid = false;  // done, or admitted for a later chunk
   Sys<N>& st = sys[tm];
   if (valid) {
     for (int q = t; q < 3 * N; q += L) {

@@ -20,9 +20,14 @@
 //                results are copied to the request's pinned host buffer
 //   completed chunks (CUDA events) hand their retired requests to pollers.
 //
-// Admission, the chunk and retirement are stream-ordered on the group's
-// stream, so a slot freed by retirement is reused by the next admission
-// without waiting for the GPU.  Groups run concurrently on their streams.
+// Each group runs the batched path's three-stream pipeline: admission and
+// the orbit producer on one stream, one chunk ahead of the transit searches
+// (a second stream) and the operator records, Jacobian consumer and
+// retirement (a third); the per-chunk buffers alternate between two halves.
+// A slot retired at chunk c is refilled at chunk c + 2 or later, whose
+// producer stream waits for chunk c's retirement, so every hand-over is
+// stream-ordered and the host never waits for the GPU.  Groups run
+// concurrently on their streams.
 // Each lane's arithmetic depends on its own system only, so a request's
 // results are bitwise the same alone or among any other requests.
 #include <cuda_runtime.h>
@@ -135,21 +140,27 @@ struct Group {
   unsigned long long kick = 0;
   int C = 0;
   GroupArgs g;
+  GroupArgs gh;  // g on the second half of the per-chunk buffers
   StageLayout lay{2, 0};
   double* stage = nullptr;
   SysOff* d_off = nullptr;
   long long *d_kbase = nullptr, *d_offtt = nullptr, *d_offdq = nullptr;
-  int* d_mask = nullptr;
+  int* d_mask = nullptr;    // admission mask (producer stream)
+  int* d_mask_r = nullptr;  // retirement mask (consumer stream)
   int* d_bad = nullptr;
   AdmitRec* d_admit = nullptr;
   int* d_list = nullptr;
   unsigned char* ring = nullptr;  // pinned upload ring: entries of [C AdmitRec][C int]
   size_t ring_entry = 0;
-  std::vector<cudaEvent_t> events;
-  cudaStream_t st = nullptr;
+  std::vector<cudaEvent_t> events;  // chunk completion, ring of max_inflight + 1
+  cudaEvent_t ev_orb[2] = {nullptr, nullptr}, ev_tr[2] = {nullptr, nullptr};
+  cudaStream_t st = nullptr;   // admission and orbit producer
+  cudaStream_t sw = nullptr;   // operator records, Jacobian consumer, retirement
+  cudaStream_t stt = nullptr;  // transit searches
   std::vector<void*> allocs;
   size_t bytes = 0;
   std::vector<Request*> slot_req;
+  std::vector<long long> free_at;  // first chunk at which a retired slot may be refilled
   std::deque<Request*> pending;
   std::deque<Inflight> inflight;
   long long chunk = 0;
@@ -311,18 +322,22 @@ int create_group(nbg_server* srv, int N, int grad, unsigned long long kick, Grou
   want(&g.m, N * S); want(&g.dqdt, 7 * N * S); want(&g.gsave, N * S); want(&g.count, N * S);
   want(&g.t0, S); want(&g.h, S); want(&g.hI, S); want(&g.nsteps, S); want(&g.ntt, S); want(&g.ti, S);
   want(&g.sysidx, S); want(&g.status, S);
-  want(&g.task_f, (size_t)g.task_cap * (12 * N + 2)); want(&g.task_i, (size_t)g.task_cap * 3);
-  want(&g.task_count, 1);
+  // per-chunk buffers: two halves (chunk c uses half c % 2)
+  const size_t nf = (size_t)g.task_cap * (12 * N + 2), ni = (size_t)g.task_cap * 3;
+  const size_t nrec = (size_t)K * g.R * S, ntrec = (size_t)K * (N - 1) * trec_size(N, 0) * S;
+  const size_t nflag = (size_t)K * (N - 1) * S, ncap = (size_t)K * 2 * npk * PCAP * S + 1;
+  const size_t nsnap = (size_t)K * snap_count(kick != 0) * 3 * N * S;
+  want(&g.task_f, 2 * nf); want(&g.task_i, 2 * ni); want(&g.task_count, 2);
   if (grad) {
-    want(&g.steprec, (size_t)K * g.R * S); want(&g.trec, (size_t)K * (N - 1) * trec_size(N, 0) * S);
-    want(&g.tflag, (size_t)K * (N - 1) * S); want(&g.tscratch, (size_t)g.R * g.tgrid);
-    want(&g.pcap, (size_t)K * 2 * npk * PCAP * S + 1);
-    want(&g.xsnap, (size_t)K * snap_count(kick != 0) * 3 * N * S);
+    want(&g.steprec, 2 * nrec); want(&g.trec, 2 * ntrec);
+    want(&g.tflag, 2 * nflag); want(&g.tscratch, (size_t)g.R * g.tgrid);
+    want(&g.pcap, 2 * ncap);
+    want(&g.xsnap, 2 * nsnap);
     want(&g.Jint, S * 6 * N * 7 * N); want(&g.Eint, S * 6 * N * 7 * N);
   }
   want(&G->stage, S * G->lay.stride);
   want(&G->d_off, S); want(&G->d_kbase, S); want(&G->d_offtt, S); want(&G->d_offdq, S);
-  want(&G->d_mask, S); want(&G->d_bad, 1); want(&G->d_admit, S); want(&G->d_list, S);
+  want(&G->d_mask, S); want(&G->d_mask_r, S); want(&G->d_bad, 1); want(&G->d_admit, S); want(&G->d_list, S);
   size_t total = 0;
   for (auto& it : items) total += (it.bytes + 255) / 256 * 256;
   if (srv->group_bytes + total > srv->cfg.hbm_budget_bytes / 2) {
@@ -351,8 +366,20 @@ int create_group(nbg_server* srv, int N, int grad, unsigned long long kick, Grou
   g.off_tt = G->d_offtt;
   g.dtdq0 = srv->heap;
   g.off_dq = G->d_offdq;
+  G->gh = g;
+  G->gh.task_f += nf; G->gh.task_i += ni; G->gh.task_count += 1;
+  if (grad) {
+    G->gh.steprec += nrec; G->gh.trec += ntrec; G->gh.tflag += nflag; G->gh.pcap += ncap; G->gh.xsnap += nsnap;
+  }
   int rc = NBG_OK;
-  if (cudaStreamCreateWithFlags(&G->st, cudaStreamNonBlocking) != cudaSuccess) rc = NBG_ECUDA;
+  if (cudaStreamCreateWithFlags(&G->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&G->sw, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&G->stt, cudaStreamNonBlocking) != cudaSuccess)
+    rc = NBG_ECUDA;
+  for (int e = 0; !rc && e < 2; e++)
+    if (cudaEventCreateWithFlags(&G->ev_orb[e], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&G->ev_tr[e], cudaEventDisableTiming) != cudaSuccess)
+      rc = NBG_ECUDA;
   G->ring_entry = (sizeof(AdmitRec) + sizeof(int)) * (size_t)C;
   const int D = srv->cfg.max_inflight;
   if (!rc && cudaHostAlloc((void**)&G->ring, G->ring_entry * (D + 1), cudaHostAllocPortable) != cudaSuccess)
@@ -368,11 +395,17 @@ int create_group(nbg_server* srv, int N, int grad, unsigned long long kick, Grou
               cudaStreamSynchronize(G->st) != cudaSuccess))
     rc = NBG_ECUDA;
   G->slot_req.assign(C, nullptr);
+  G->free_at.assign(C, 0);
   if (rc) {
     cudaGetLastError();
     for (auto e : G->events) cudaEventDestroy(e);
+    for (int e = 0; e < 2; e++) {
+      if (G->ev_orb[e]) cudaEventDestroy(G->ev_orb[e]);
+      if (G->ev_tr[e]) cudaEventDestroy(G->ev_tr[e]);
+    }
     if (G->ring) cudaFreeHost(G->ring);
-    if (G->st) cudaStreamDestroy(G->st);
+    for (cudaStream_t s2 : {G->st, G->sw, G->stt})
+      if (s2) cudaStreamDestroy(s2);
     cudaFree(base);
     delete G;
     return set_error(NBG_ECUDA, "server: stream / event / pinned ring creation failed for a group of n = %d", N);
@@ -383,10 +416,16 @@ int create_group(nbg_server* srv, int N, int grad, unsigned long long kick, Grou
 }
 
 void destroy_group(Group* G) {
-  if (G->st) cudaStreamSynchronize(G->st);
+  for (cudaStream_t s2 : {G->st, G->sw, G->stt})
+    if (s2) cudaStreamSynchronize(s2);
   for (auto e : G->events) cudaEventDestroy(e);
+  for (int e = 0; e < 2; e++) {
+    if (G->ev_orb[e]) cudaEventDestroy(G->ev_orb[e]);
+    if (G->ev_tr[e]) cudaEventDestroy(G->ev_tr[e]);
+  }
   if (G->ring) cudaFreeHost(G->ring);
-  if (G->st) cudaStreamDestroy(G->st);
+  for (cudaStream_t s2 : {G->st, G->sw, G->stt})
+    if (s2) cudaStreamDestroy(s2);
   for (void* p : G->allocs) cudaFree(p);
   delete G;
 }
@@ -429,8 +468,8 @@ int service_group(nbg_server* srv, int gi) {
     if (!f.retired.empty()) srv->cv_done.notify_all();
   }
   if ((int)G->inflight.size() >= D) return 0;
-  // ---- admission (host decisions; the slots' previous occupants, if any,
-  // were retired earlier on this stream)
+  // ---- admission (host decisions; a slot's previous occupant, if any, was
+  // retired at chunk c - 2 or earlier, and the producer stream waits for it)
   const long long c = G->chunk;
   const int e = (int)(c % (D + 1));
   AdmitRec* up = (AdmitRec*)(G->ring + (size_t)e * G->ring_entry);
@@ -439,7 +478,7 @@ int service_group(nbg_server* srv, int gi) {
   {
     int free_slot = 0;
     while (!G->pending.empty()) {
-      while (free_slot < C && G->slot_req[free_slot]) free_slot++;
+      while (free_slot < C && (G->slot_req[free_slot] || G->free_at[free_slot] > c)) free_slot++;
       if (free_slot >= C) break;
       Request* r = G->pending.front();
       size_t off;
@@ -467,10 +506,15 @@ int service_group(nbg_server* srv, int gi) {
     srv->stats.hbm_outputs_in_use = srv->arena.used * sizeof(double);
   }
   if (G->active == 0) return 0;
-  cudaStream_t st = G->st;
+  cudaStream_t st = G->st, sw = G->sw, stt = G->stt;
+  const int par = (int)(c & 1);
+  const GroupArgs& gc = par ? G->gh : g;  // this chunk's half of the per-chunk buffers
   const StageLayout& L = G->lay;
   const size_t stride = L.stride;
   long long launches = 0;
+  // chunk c reuses chunk c - 2's buffer half and may refill slots retired at
+  // chunk c - 2 or earlier: the producer stream waits for that chunk's end
+  if (c >= 2) NBG_CUDA(cudaStreamWaitEvent(st, G->events[(c - 2) % (D + 1)], 0));
   if (!admitted.empty()) {
     const int na = (int)admitted.size();
     for (int q = 0; q < na; q++) {
@@ -508,16 +552,25 @@ int service_group(nbg_server* srv, int gi) {
     launch_group_seed(N, gm, st);
     launches++;
   }
-  // ---- one chunk of every active slot
-  NBG_CUDA(cudaMemsetAsync(g.task_count, 0, sizeof(int), st));
+  // ---- one chunk of every active slot: the producer on st, then the
+  // searches on stt beside the operator records on sw, then the consumer
+  NBG_CUDA(cudaMemsetAsync(gc.task_count, 0, sizeof(int), st));
   int rc;
-  if ((rc = launch_group_orbit(N, g, (int)c, st))) return rc;
-  if ((rc = launch_group_transit(N, g, (int)c, st))) return rc;
+  if ((rc = launch_group_orbit(N, gc, (int)c, st))) return rc;
+  NBG_CUDA(cudaEventRecord(G->ev_orb[par], st));
+  NBG_CUDA(cudaStreamWaitEvent(stt, G->ev_orb[par], 0));
+  NBG_CUDA(cudaStreamWaitEvent(sw, G->ev_orb[par], 0));
+  if ((rc = launch_group_transit(N, gc, (int)c, stt))) return rc;
+  NBG_CUDA(cudaEventRecord(G->ev_tr[par], stt));
   launches += 2;
   if (G->grad) {
-    if ((rc = launch_group_operators(N, g, (int)c, st))) return rc;
-    if ((rc = launch_group_jacobian(N, g, (int)c, st))) return rc;
-    launches += 3;
+    if ((rc = launch_group_operators(N, gc, (int)c, sw))) return rc;
+    launches += 2;
+  }
+  NBG_CUDA(cudaStreamWaitEvent(sw, G->ev_tr[par], 0));
+  if (G->grad) {
+    if ((rc = launch_group_jacobian(N, gc, (int)c, sw))) return rc;
+    launches += 1;
   }
   // ---- retirement of the slots whose last step ran in this chunk
   Inflight f;
@@ -531,34 +584,36 @@ int service_group(nbg_server* srv, int gi) {
     }
   }
   if (nr) {
-    NBG_CUDA(cudaMemcpyAsync(G->d_list, ulist, sizeof(int) * nr, cudaMemcpyHostToDevice, st));
-    NBG_CUDA(cudaMemsetAsync(G->d_mask, 0xff, sizeof(int) * C, st));
-    mark_kernel<<<(nr + 127) / 128, 128, 0, st>>>(nr, G->d_list, G->d_mask);
+    // on the consumer stream, after the chunk's consumer and searches
+    NBG_CUDA(cudaMemcpyAsync(G->d_list, ulist, sizeof(int) * nr, cudaMemcpyHostToDevice, sw));
+    NBG_CUDA(cudaMemsetAsync(G->d_mask_r, 0xff, sizeof(int) * C, sw));
+    mark_kernel<<<(nr + 127) / 128, 128, 0, sw>>>(nr, G->d_list, G->d_mask_r);
     double* sg = G->stage;
-    launch_unpack_state(N, C, G->grad, G->d_mask, G->d_off, sg + L.X, sg + L.V, sg + L.XE, sg + L.VE, sg + L.DQ,
-                        (long long*)(sg + L.CNT), g, st);
+    launch_unpack_state(N, C, G->grad, G->d_mask_r, G->d_off, sg + L.X, sg + L.V, sg + L.XE, sg + L.VE, sg + L.DQ,
+                        (long long*)(sg + L.CNT), g, sw);
     launches += 2;
     if (G->grad) {
-      launch_unpack_jac(N, C, G->d_mask, G->d_off, sg + L.JJ, sg + L.EE, g, st);
+      launch_unpack_jac(N, C, G->d_mask_r, G->d_off, sg + L.JJ, sg + L.EE, g, sw);
       launch_dtdelements(nr, G->d_list, G->d_off, srv->heap, sg + L.JI, srv->heap, (const long long*)(sg + L.CNT),
-                         true, st);
+                         true, sw);
       launches += 2;
     }
-    deactivate_kernel<<<(nr + 127) / 128, 128, 0, st>>>(nr, G->d_list, g.sysidx);
+    deactivate_kernel<<<(nr + 127) / 128, 128, 0, sw>>>(nr, G->d_list, g.sysidx);
     launches++;
     for (Request* r : f.retired) {
       NBG_CUDA(cudaMemcpyAsync(r->host, G->stage + (size_t)r->slot * stride, sizeof(double) * stride,
-                               cudaMemcpyDeviceToHost, st));
+                               cudaMemcpyDeviceToHost, sw));
       NBG_CUDA(cudaMemcpyAsync(r->host + r->stage_n, srv->heap + r->heap_off, sizeof(double) * r->heap_n,
-                               cudaMemcpyDeviceToHost, st));
+                               cudaMemcpyDeviceToHost, sw));
       NBG_CUDA(cudaMemcpyAsync(r->host + r->stage_n + r->heap_n, g.status + r->slot, sizeof(uint32_t),
-                               cudaMemcpyDeviceToHost, st));
+                               cudaMemcpyDeviceToHost, sw));
       G->slot_req[r->slot] = nullptr;
+      G->free_at[r->slot] = c + 2;  // refilled once this chunk's retirement has run
       G->active--;
     }
   }
   NBG_CUDA(cudaGetLastError());
-  NBG_CUDA(cudaEventRecord(f.ev, st));
+  NBG_CUDA(cudaEventRecord(f.ev, sw));
   G->inflight.push_back(std::move(f));
   G->chunk++;
   {
