@@ -37,6 +37,10 @@ import time
 
 import numpy as np
 
+# 32 hardware work queues for the library's per-group streams, set before
+# torch creates the CUDA context (the library and package set the same default)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG_DIR = os.path.join(ROOT, "nbodygradient.jl_gb300")
 

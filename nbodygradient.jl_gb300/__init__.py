@@ -17,8 +17,15 @@ the arrays.  There is no CPU fallback: without the CUDA library or a GPU the
 calls raise NbgError.
 """
 import math
+import os
 
 import numpy as np
+
+# Each group of a batch runs on three CUDA streams of its own: ask the driver
+# for 32 hardware work queues (the default 8 makes groups' streams share
+# queues and serialise) before the process creates its CUDA context.  The
+# library does the same when it is loaded; a caller's own setting is kept.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 from . import _lib, build, workloads
 from ._lib import Context, NbgError, SystemDesc, default_context, device_info

@@ -9,6 +9,10 @@ import sys
 
 import pytest
 
+# as the package does: 32 hardware work queues for the per-group streams,
+# before any test creates the CUDA context
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PKG_DIR = os.path.join(ROOT, "nbodygradient.jl_gb300")
 sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
