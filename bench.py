@@ -432,6 +432,7 @@ def main():
     clk = ClockSampler(local_rank)
     clk.start()
     launches = 0
+    host_ms = 0.0
     # per-kernel CUDA-event pairs on each kernel's own stream, summed over the
     # timed steps: the roofline's kernel durations come from the timed region
     # one event pair per timed step, around the Jacobian consumer's launch of
@@ -448,6 +449,7 @@ def main():
     for _ in range(args.steps):
         step()
         launches += ctx.last_launch_count()
+        host_ms += ctx.last_host_ms()
         kt += np.array(ctx.last_timing())
         kn += np.array(ctx.last_kernel_stats(), dtype=np.int64)
     e1.record()
@@ -532,6 +534,7 @@ def main():
             "e2e": {"value": e2e_val, "unit": "system-steps/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.mean(e2e_ms)) if e2e_ms else None},
             "gpu_launches": int(launches),
+            "host_enqueue_ms_per_step": host_ms / args.steps,
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                          "kernel": "jacobian_chunk_kernel", "peak_source": "measured live (nbg_fp64_peak, DFMA)",

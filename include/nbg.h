@@ -425,6 +425,11 @@ int nbg_last_kernel_stats(nbg_context* ctx, int64_t* orbit_launches, int64_t* ja
 /* Number of kernels launched by the last call. */
 int64_t nbg_last_launch_count(nbg_context* ctx);
 
+/* Host (wall-clock) time the last batched call spent enqueueing its chunk
+ * loop -- the launch overhead a CUDA graph of the loop could save.  No
+ * counterpart in the reference; a measurement helper. */
+int nbg_last_host_time(nbg_context* ctx, double* enqueue_ms);
+
 /* Measured FP64 FMA throughput of the context's device (TFLOP/s, FMA = 2
  * flops): the roofline denominator for the FP64-bound kernels.  No
  * counterpart in the reference; a measurement helper. */

@@ -32,7 +32,7 @@ EXPORTS = (
     "nbg_integrate_transits", "nbg_batch_integrate_transits", "nbg_batch_integrate_transits_device",
     "nbg_set_tuning", "nbg_last_timing", "nbg_last_launch_count", "nbg_fp64_peak",
     "nbg_set_profiling", "nbg_last_kernel_stats", "nbg_set_orbit_lanes", "nbg_set_orbit_team",
-    "nbg_set_producer_layout",
+    "nbg_set_producer_layout", "nbg_last_host_time",
     "nbg_batch_integrate_transits_noalloc",
     "nbg_integrate", "nbg_integrate_steps", "nbg_batch_integrate",
     "nbg_integrate_transit_parameters", "nbg_batch_integrate_transit_parameters",
@@ -144,6 +144,7 @@ def load(build_if_missing=True):
     L.nbg_set_orbit_lanes.argtypes = [_VP, ctypes.c_int]
     L.nbg_set_orbit_team.argtypes = [_VP, ctypes.c_int]
     L.nbg_set_producer_layout.argtypes = [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.nbg_last_host_time.argtypes = [_VP, _D]
     L.nbg_last_kernel_stats.argtypes = [_VP, _I64, _I64]
     L.nbg_server_start.argtypes = [ctypes.c_int, ctypes.POINTER(ServerConfig), ctypes.POINTER(_VP)]
     L.nbg_server_enqueue.argtypes = [_VP, ctypes.POINTER(SystemDesc), ctypes.c_double, _D, _D, _D, _D, _D, _D, _D,
@@ -210,6 +211,12 @@ class Context:
         a, b, c, d = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         check(load().nbg_last_timing(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(d)))
         return a.value, b.value, c.value, d.value
+
+    def last_host_ms(self):
+        """Host time (ms) the last batched call spent enqueueing its chunk loop."""
+        v = ctypes.c_double()
+        check(load().nbg_last_host_time(self._h, ctypes.byref(v)))
+        return v.value
 
     def last_launch_count(self):
         return int(load().nbg_last_launch_count(self._h))

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -243,6 +244,7 @@ struct nbg_context {
   int prod_warps = 1, prod_smem_kb = 0, guard_smem_kb = 0;  // orbit producer block layout
   int sm_count = 0;
   double last_total_ms = 0, last_orbit_ms = 0, last_jac_ms = 0, last_transit_ms = 0, last_ops_ms = 0;
+  double last_host_ms = 0;  // host time spent enqueueing the chunk loop
   long long last_launches = 0, last_orbit_launches = 0, last_jac_launches = 0;
   int profile = 0;
   std::vector<cudaEvent_t> prof_events;  // pairs around each timed launch
@@ -650,6 +652,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
   };
   ctx->last_orbit_launches = ctx->last_jac_launches = 0;
   NBG_CUDA(cudaEventRecord(ctx->ev0, st));
+  const auto host0 = std::chrono::steady_clock::now();
   if (!ctx->overlap) {
     for (long long c = 0; c < nchunks; c++) {
       for (size_t q = 0; q < gargs.size(); q++) {
@@ -738,6 +741,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
   }
   NBG_CUDA(cudaGetLastError());
   NBG_CUDA(cudaEventRecord(ctx->ev1, st));
+  ctx->last_host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host0).count();
   // ---- outputs
   for (auto& g : gargs) {
     int pb = (g.S + 127) / 128;
@@ -1244,6 +1248,12 @@ int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double
 }
 
 int64_t nbg_last_launch_count(nbg_context* ctx) { return ctx ? ctx->last_launches : -1; }
+
+int nbg_last_host_time(nbg_context* ctx, double* enqueue_ms) {
+  if (!ctx || !enqueue_ms) return set_error(NBG_EINVAL, "NULL argument");
+  *enqueue_ms = ctx->last_host_ms;
+  return NBG_OK;
+}
 
 int nbg_fp64_peak(nbg_context* ctx, double* tflops) {
   if (!ctx || !tflops) return set_error(NBG_EINVAL, "NULL argument");
