@@ -65,3 +65,41 @@ def test_null_arguments_are_rejected_without_a_gpu():
 def test_context_creation_fails_loudly_without_gpu():
     with pytest.raises(nbg.NbgError):
         nbg.Context(0)
+
+
+def test_new_entry_points_reject_null_arguments_without_a_gpu():
+    L = nbg._lib.load()
+    E = nbg._lib.NBG_EINVAL
+    assert L.nbg_set_producer_layout(None, 4, 200, 32) == E
+    assert L.nbg_set_orbit_team(None, 1) == E
+    assert L.nbg_last_host_time(None, None) == E
+    assert L.nbg_integrate(None, 3, 0.5, 10.0, 1, *([None] * 10)) == E
+    assert L.nbg_integrate_steps(None, 3, 0.5, 10, 1, *([None] * 10)) == E
+    assert L.nbg_integrate_cartesian(None, 3, 0.5, 10.0, 5, *([None] * 14)) == E
+    assert L.nbg_batch_init_nbody(None, 1, None, None, None, None, None, None, None) == E
+    assert L.nbg_autotune_device(None, 1, None, *([None] * 11), 64, None, 0, None) == E
+    assert L.nbg_integrate_transit_parameters(None, 3, 0, 0.5, 10.0, 1, *([None] * 11), 10, None, None, None,
+                                              None) == E
+    assert L.nbg_server_enqueue(None, None, 0.0, *([None] * 10), None) == E
+    assert L.nbg_server_stats(None, None) == E
+    assert L.nbg_server_stop(None) == nbg._lib.NBG_OK
+
+
+def test_transit_parameters_and_cartesian_output_shapes():
+    from nbg import workloads as W
+    el, _, _ = W.plain_3body(0)
+    ic = W.ic_of(el)
+    tp = nbg.TransitParameters(1000.0, ic)
+    assert tp.ntt == 103 and tp.ttbv.shape == (3, 3, 103) and tp.dtbvdq0.shape == (3, 3, 103, 7, 3)
+    assert tp.occs == [2, 3]
+    with pytest.raises(ValueError):
+        nbg.TransitParameters(1000.0, ic, ntt=5)
+    o = nbg.CartesianOutput(3, 7)
+    assert o.x.shape == (7, 3, 3) and o.jac_step.shape == (7, 21, 21) and len(o.states) == 7
+    assert nbg.CartesianOutput(3, 7, jac=False).jac_step is None
+
+
+@pytest.mark.skipif(has_gpu(), reason="checks the no-GPU error path")
+def test_server_start_fails_loudly_without_gpu():
+    with pytest.raises(nbg.NbgError):
+        nbg.Server()
