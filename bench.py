@@ -240,6 +240,9 @@ def run_reference(args, nbg, rank):
             vals.append((v, used, t))
     value = float(np.mean([v for v, _, _ in vals]))
     used = vals[-1][1]
+    # the same restatement on one host thread, on a smaller sample
+    v1, _, used1, t1 = cpu_baseline(nbg, states, timings, hs, tms, nsteps, target_s=min(4.0, args.ref_seconds),
+                                    nthreads=1)
     line = {
         "impl": "reference", "metric": "system_steps_per_s", "value": value, "unit": "system-steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -250,6 +253,8 @@ def run_reference(args, nbg, rank):
                          "sample": "%d systems of %s per step (C++ restatement of the reference, "
                                    "Julia unavailable)" % (used, args.workload)},
         "e2e": {"value": value, "unit": "system-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_1core": {"value": v1, "unit": "system-steps/s", "cores": 1,
+                      "sample": "%d systems of %s, %.1f s on one host thread" % (used1, args.workload, t1)},
     }
     print(json.dumps(line), flush=True)
 
@@ -304,7 +309,7 @@ def serve_stream(nbg, srv, pool, rate, nreq, seed, timeout_s):
 
 
 def run_serve(args, nbg):
-    """Serving (C4): Poisson streams of single systems drawn as batch_uneven,
+    """Serving: Poisson streams of single systems drawn as batch_uneven,
     50 % grad=true; system-steps/s and p50/p99 latency per body count."""
     W = nbg.workloads
     els, hs, tms = W.batch_uneven(args.serve_pool, args.seed + 11)
@@ -365,7 +370,7 @@ def main():
                     help="steps per system of the shorter autotuner trial (the longer runs twice as many)")
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--serve", action="store_true", help="serving (C4): Poisson request streams, then exit")
+    ap.add_argument("--serve", action="store_true", help="serving: Poisson request streams of batch_uneven draws, then exit")
     ap.add_argument("--serve-rates", default="4,16,64,0", help="request rates per second (0 = all at once)")
     ap.add_argument("--serve-requests", type=int, default=256)
     ap.add_argument("--serve-pool", type=int, default=512)

@@ -5,15 +5,15 @@ distributions below, built with ElementsIC(t0 = 0, H = N fully nested,
 elements), elements rows (m, P, t0_transit, e cos w, e sin w, I, Omega) and a
 star row (M*, 0, ..., 0).
 
-  plain_3body   (C0) N=3, M*=1, m ~ U(3e-6, 3e-5), P = (10.0, 20.1),
+  plain_3body   N=3, M*=1, m ~ U(3e-6, 3e-5), P = (10.0, 20.1),
                 e ~ U(0, 0.05), w, t0 uniform over the orbit, I = pi/2,
                 Omega = 0; h = P1/20 = 0.5, tmax = 1000 -> 2000 steps
-  batch_3body   (C1) 4096 Gaussian perturbations (1e-4 relative on masses,
-                periods, e cos w, e sin w, t0) of one C0 draw
-  batch_8body   (C2) 1024 x N=8, M*=0.09, m ~ U(1e-6, 1.5e-5),
+  batch_3body   4096 Gaussian perturbations (1e-4 relative on masses,
+                periods, e cos w, e sin w, t0) of one plain_3body draw
+  batch_8body   1024 x N=8, M*=0.09, m ~ U(1e-6, 1.5e-5),
                 P = (1.5, 2.4, 4.0, 6.1, 9.2, 12.4, 18.8)(1 + 1e-3 N(0,1)),
                 e ~ U(0, 0.01), I = pi/2; h = 0.06, tmax = 1600
-  batch_uneven  (C3) N ~ U{2..10}, P log-uniform 1..100 d sorted and
+  batch_uneven  N ~ U{2..10}, P log-uniform 1..100 d sorted and
                 redrawn until adjacent pairs are separated by more than
                 HILL_DELTA mutual Hill radii, m log-uniform 1e-6..1e-4,
                 e ~ U(0, 0.1), I = pi/2 + N(0, 0.01), Omega = 0,
@@ -37,7 +37,7 @@ def _ecc_pair(rng, emax, size=None):
 
 
 def plain_3body(seed=0):
-    """C0: one 3-body system near 2:1 resonance.  Returns (elements, h, tmax)."""
+    """One 3-body system near 2:1 resonance.  Returns (elements, h, tmax)."""
     rng = np.random.default_rng(seed)
     el = np.zeros((3, 7))
     el[0, 0] = 1.0
@@ -49,7 +49,7 @@ def plain_3body(seed=0):
 
 
 def batch_3body(nsys=4096, seed=0):
-    """C1: nsys perturbations of one C0 draw.  Returns (list of elements, h, tmax)."""
+    """nsys perturbations of one plain_3body draw.  Returns (list of elements, h, tmax)."""
     base, h, tmax = plain_3body(seed)
     rng = np.random.default_rng(seed + 1)
     out = []
@@ -62,7 +62,7 @@ def batch_3body(nsys=4096, seed=0):
 
 
 def batch_8body(nsys=1024, seed=0):
-    """C2: nsys 8-body TRAPPIST-like systems.  Returns (list of elements, h, tmax)."""
+    """nsys 8-body TRAPPIST-like systems.  Returns (list of elements, h, tmax)."""
     rng = np.random.default_rng(seed + 2)
     P0 = np.array([1.5, 2.4, 4.0, 6.1, 9.2, 12.4, 18.8])
     out = []
@@ -91,7 +91,7 @@ def _hill_ok(P, m, mstar):
 
 
 def batch_uneven(nsys=2048, seed=0, nmin=2, nmax=10):
-    """C3: mixed body counts and durations.  Returns (list of elements, list of h, list of tmax)."""
+    """Mixed body counts and durations.  Returns (list of elements, list of h, list of tmax)."""
     rng = np.random.default_rng(seed + 3)
     els, hs, tmaxs = [], [], []
     for _ in range(nsys):

@@ -118,7 +118,7 @@ def test_served_results_match_oracle():
 
 
 def test_full_length_requests_and_latency_record():
-    """Two full C0 requests (2000 steps) in the mix with short ones; latency fields are consistent."""
+    """Two full plain_3body requests (2000 steps) in the mix with short ones; latency fields are consistent."""
     el, h, tmax = W.plain_3body(0)
     longs = []
     for _ in range(2):
