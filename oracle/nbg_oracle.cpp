@@ -489,4 +489,43 @@ int oracle_fd_init_nbody(int n, double t0, const double* elements, const double*
   return 0;
 }
 
+// kepler_init with its 7x7 Jacobian (kepler_init.jl:66-210) for one
+// Keplerian, in double (quad = 0) or in quad precision (quad = 1, outputs
+// rounded to double).  el = (P, t0, e cos w, e sin w, I, Omega).
+int oracle_kepler_init(double time, double mass, const double* el, int quad_prec, double* x, double* v,
+                       double* jac) {
+  if (quad_prec) {
+    quad e[6], xq[3], vq[3], jq[49];
+    for (int q = 0; q < 6; q++) e[q] = quad(el[q]);
+    kepler_init<quad>(quad(time), quad(mass), e, xq, vq, jq);
+    for (int q = 0; q < 3; q++) { x[q] = (double)xq[q]; v[q] = (double)vq[q]; }
+    for (int q = 0; q < 49; q++) jac[q] = (double)jq[q];
+  } else {
+    kepler_init<double>(time, mass, el, x, v, jac);
+  }
+  return 0;
+}
+
+// Numerical d(x, v, m) / d(elements, m) of kepler_init
+// (test/test_kepler_init.jl:34-76): two-sided differences in quad precision
+// with absolute steps dq[7] (P, t0, e cos w, e sin w, I, Omega, mass).
+int oracle_fd_kepler_init(double time, double mass, const double* el, const double* dq, double* jac_num) {
+  for (int q = 0; q < 49; q++) jac_num[q] = 0.0;
+  for (int j = 0; j < 7; j++) {
+    quad ep[6], em[6], mp = quad(mass), mm = quad(mass), xp[3], vp[3], xm[3], vm[3], jt[49];
+    for (int q = 0; q < 6; q++) ep[q] = em[q] = quad(el[q]);
+    const quad d = quad(dq[j]);
+    if (j < 6) { ep[j] = ep[j] + d; em[j] = em[j] - d; }
+    else { mp = mp + d; mm = mm - d; }
+    kepler_init<quad>(quad(time), mp, ep, xp, vp, jt);
+    kepler_init<quad>(quad(time), mm, em, xm, vm, jt);
+    for (int k = 0; k < 3; k++) {
+      jac_num[k + 7 * j] = (double)(quad(0.5) * (xp[k] - xm[k]) / d);
+      jac_num[3 + k + 7 * j] = (double)(quad(0.5) * (vp[k] - vm[k]) / d);
+    }
+  }
+  jac_num[6 + 7 * 6] = 1.0;
+  return 0;
+}
+
 }  // extern "C"

@@ -231,6 +231,20 @@ def fd_dtbvdelements(elements, t0, h, tmax, ti, ntt, dq0=1e-10, H=None, nthreads
     return out
 
 
+def kepler_init(time, mass, el6, quad=False):
+    """kepler_init with its 7x7 Jacobian: returns x (3), v (3), jac (7, 7)."""
+    e = f64(el6)
+    x, v, jac = np.zeros(3), np.zeros(3), np.zeros((7, 7), order="F")
+    lib().oracle_kepler_init(ctypes.c_double(time), ctypes.c_double(mass), _p(e), int(quad), _p(x), _p(v), _p(jac))
+    return x, v, jac
+
+
+def fd_kepler_init(time, mass, el6, dq):
+    jac = np.zeros((7, 7), order="F")
+    lib().oracle_fd_kepler_init(ctypes.c_double(time), ctypes.c_double(mass), _p(f64(el6)), _p(f64(dq)), _p(jac))
+    return jac
+
+
 def fd_init_nbody(elements, t0, dq, dq_star_mass=1e-15, H=None):
     el = f64(elements)
     n = el.shape[0]

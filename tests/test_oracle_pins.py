@@ -269,6 +269,25 @@ def test_transit_timing_derivatives_synthetic():
     assert close(np.arcsinh(tt.dtdelements), np.arcsinh(num))
 
 
+def test_kepler_init_jacobian():
+    """test/test_kepler_init.jl: kepler_init's 7x7 Jacobian for ten random orbits (P = 1.5, t0 ~ U(0, P),
+    e cos w and e sin w ~ N(0, 1) redrawn until e < 0.2, I and Omega ~ U(0, pi), mass 1, time 2.4) against
+    two-sided quad differences (steps 1e-15, as the reference's BigFloat ones) and against the same formulae
+    evaluated in quad; isapprox with maxabs norm at Julia's default rtol."""
+    rng = np.random.default_rng(17)
+    period, mass, time = 1.5, 1.0, 2.4
+    for _ in range(10):
+        el = np.ones(6)
+        while el[2] ** 2 + el[3] ** 2 >= 0.2 ** 2:
+            el = np.array([period, rng.uniform() * period, rng.standard_normal(), rng.standard_normal(),
+                           rng.uniform() * np.pi, rng.uniform() * np.pi])
+        _, _, jac = O.kepler_init(time, mass, el)
+        _, _, jac_q = O.kepler_init(time, mass, el, quad=True)
+        num = O.fd_kepler_init(time, mass, el, [1e-15] * 7)
+        assert close(jac, num)
+        assert close(jac, jac_q)
+
+
 def test_init_nbody_jacobian(ref_elements):
     """test/test_init_nbody.jl: jac_init against two-sided differences (steps 1e-12 / 1e-10)."""
     t0 = 7257.93115525 - 7300.0
