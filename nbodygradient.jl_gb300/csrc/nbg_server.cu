@@ -90,9 +90,23 @@ __global__ void mark_kernel(int n, const int* list, int* mask) {
   if (i < n) mask[list[i]] = list[i];
 }
 
-__global__ void deactivate_kernel(int n, const int* list, int* sysidx) {
+// kbase of a slot that holds no request.  A byte-wise fill of 0x3f makes it
+// (cudaMemsetAsync), and it puts every chunk's first step of the slot far
+// below zero, so kernels skip the slot whatever mix of old and new slot
+// settings they read while a later chunk's admission rewrites them.
+constexpr long long KBASE_FREE = 0x3f3f3f3f3f3f3f3fLL;
+
+// Retirement: the slot is inactive (sysidx = -1) and its kbase leaves the
+// request's steps.  Chunk c + 1's kernels may run while chunk c + 2 admits a
+// new request into the slot (admit_kernel, on another stream): if one reads
+// the new sysidx and nsteps beside the retired kbase, its first step is still
+// negative and it skips the slot.
+__global__ void deactivate_kernel(int n, const int* list, int* sysidx, long long* kbase) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) sysidx[list[i]] = -1;
+  if (i < n) {
+    sysidx[list[i]] = -1;
+    kbase[list[i]] = KBASE_FREE;
+  }
 }
 
 // Per-slot staging layout (doubles) of a request in the caller's layout:
@@ -391,7 +405,7 @@ int create_group(nbg_server* srv, int N, int grad, unsigned long long kick, Grou
   }
   if (!rc && (cudaMemsetAsync(g.sysidx, 0xff, sizeof(int) * S, G->st) != cudaSuccess ||
               cudaMemsetAsync(g.nsteps, 0, sizeof(long long) * S, G->st) != cudaSuccess ||
-              cudaMemsetAsync(G->d_kbase, 0, sizeof(long long) * S, G->st) != cudaSuccess ||
+              cudaMemsetAsync(G->d_kbase, 0x3f, sizeof(long long) * S, G->st) != cudaSuccess ||  // KBASE_FREE
               cudaStreamSynchronize(G->st) != cudaSuccess))
     rc = NBG_ECUDA;
   G->slot_req.assign(C, nullptr);
@@ -598,7 +612,7 @@ int service_group(nbg_server* srv, int gi) {
                          true, sw);
       launches += 2;
     }
-    deactivate_kernel<<<(nr + 127) / 128, 128, 0, sw>>>(nr, G->d_list, g.sysidx);
+    deactivate_kernel<<<(nr + 127) / 128, 128, 0, sw>>>(nr, G->d_list, g.sysidx, G->d_kbase);
     launches++;
     for (Request* r : f.retired) {
       NBG_CUDA(cudaMemcpyAsync(r->host, G->stage + (size_t)r->slot * stride, sizeof(double) * stride,

@@ -100,6 +100,29 @@ def test_mix_is_bitwise_alone_and_batched():
         assert_same(mix[q], (s, tt))
 
 
+def test_refilled_slots_are_bitwise_alone():
+    """96 short 3-body gradient requests in one group of 32 slots: slots retire and are refilled two chunks later
+    while the previous chunk's operator and Jacobian kernels still run on the group's other streams; every result
+    is bitwise the one of the same request alone (nbg_integrate_transits)."""
+    rng = np.random.default_rng(23)
+    els, hs, _ = W.batch_uneven(96, seed=23, nmin=3, nmax=3)
+    reqs = []
+    for el, h in zip(els, hs):
+        tmax = float(h * rng.integers(20, 81))
+        ic = W.ic_of(el)
+        reqs.append((nbg.State(ic), nbg.TransitTiming(tmax, ic), nbg.Integrator(nbg.ahl21, h, 0.0, tmax), True))
+    with nbg.Server(slots_per_group=32, chunk_steps=8, max_inflight=3) as srv:
+        mix, infos = serve_mix(srv, reqs, jitter_ms=0.2, seed=4)
+        st = srv.stats()
+    assert all(i["rc"] == 0 for i in infos)
+    assert st["groups"] == 1 and st["admitted"] == len(reqs)  # 96 requests through 32 slots: slots were reused
+    assert max(i["queue_ms"] for i in infos) > 0.0
+    for q, r in enumerate(reqs):
+        s1, tt1, intr, _ = fresh(r)
+        intr(s1, tt1, grad=True)
+        assert_same(mix[q], (s1, tt1))
+
+
 def test_served_results_match_oracle():
     reqs = make_requests(8, seed=5)
     with nbg.Server(slots_per_group=32, chunk_steps=8) as srv:
