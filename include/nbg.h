@@ -155,7 +155,8 @@ int nbg_batch_init_nbody_device(nbg_context* ctx, int nsys, const int32_t* n, co
                                 const double* elements, const double* H, double* x, double* v, double* jac_init);
 
 /*
- * Batched form: nsys independent systems integrated in one plan.  Each
+ * Batched form: nsys >= 1 independent systems integrated in one plan (an
+ * empty batch returns NBG_EINVAL, as does every batched entry point).  Each
  * system's arrays are laid out exactly as for nbg_integrate_transits and
  * concatenated system after system in every packed buffer (so the offset of
  * system s in `x` is sum_{q<s} 3 n_q, in `jac_step` sum_{q<s} (7 n_q)^2, in
