@@ -40,7 +40,7 @@ def nvcc():
 
 
 def _sources():
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h"))) + \
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h", ".hpp"))) + \
         [os.path.join(INCLUDE, "nbg.h")]
 
 

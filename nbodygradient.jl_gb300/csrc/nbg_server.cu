@@ -48,6 +48,7 @@
 #include <vector>
 
 #include "../../include/nbg.h"
+#include "nbg_arena.hpp"
 #include "nbg_internal.cuh"
 
 using namespace nbg;
@@ -179,51 +180,6 @@ struct Group {
   std::deque<Inflight> inflight;
   long long chunk = 0;
   int active = 0;
-};
-
-// First-fit allocator over the output arena (offsets in doubles).
-struct Arena {
-  size_t size = 0;
-  std::map<size_t, size_t> free_;  // offset -> length
-  size_t used = 0;
-  void init(size_t n) {
-    size = n;
-    free_.clear();
-    if (n) free_[0] = n;
-    used = 0;
-  }
-  static size_t round(size_t n) { return (std::max<size_t>(n, 1) + 31) / 32 * 32; }  // 256-byte blocks
-  bool alloc(size_t n, size_t* off) {
-    n = round(n);
-    for (auto it = free_.begin(); it != free_.end(); ++it) {
-      if (it->second >= n) {
-        *off = it->first;
-        const size_t rest = it->second - n, at = it->first + n;
-        free_.erase(it);
-        if (rest) free_[at] = rest;
-        used += n;
-        return true;
-      }
-    }
-    return false;
-  }
-  void release(size_t off, size_t n) {
-    n = round(n);
-    used -= n;
-    auto it = free_.emplace(off, n).first;
-    auto nx = std::next(it);
-    if (nx != free_.end() && it->first + it->second == nx->first) {
-      it->second += nx->second;
-      free_.erase(nx);
-    }
-    if (it != free_.begin()) {
-      auto pv = std::prev(it);
-      if (pv->first + pv->second == it->first) {
-        pv->second += it->second;
-        free_.erase(it);
-      }
-    }
-  }
 };
 
 // Pinned host buffers, recycled by power-of-two size class.
@@ -681,7 +637,7 @@ void server_main(nbg_server* srv) {
       } else {
         gi = it->second;
       }
-      if (r->heap_n > srv->arena.size) {
+      if (Arena::round(r->heap_n) > srv->arena.size) {
         char buf[256];
         snprintf(buf, sizeof(buf), "server: the request needs %zu output bytes, the output arena holds %zu",
                  r->heap_n * sizeof(double), srv->arena.size * sizeof(double));
