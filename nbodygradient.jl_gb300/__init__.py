@@ -213,6 +213,8 @@ class Integrator:
                 tt = float(s.t[0] + self.tmax)
             if isinstance(tt, (int, np.integer)) and not isinstance(tt, bool):
                 _lib.check(L.nbg_integrate_steps(ctx.handle, s.n, self.h, int(tt), int(bool(grad)), *args))
+                if self.h < 0:  # intr(s, N) leaves intr.h positive (Integrator.jl:228-229)
+                    self.h = -self.h
             else:
                 _lib.check(L.nbg_integrate(ctx.handle, s.n, self.h, float(tt), int(bool(grad)), *args))
             return None

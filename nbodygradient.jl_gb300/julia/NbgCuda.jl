@@ -99,6 +99,7 @@ function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, N::Int64;
                    s.t, s.x, s.v, s.m, s.xerror, s.verror, s.jac_step, s.jac_error, s.dqdt, s.pair)
     end
     rc == 0 || error("libnbg_cuda: ", last_error())
+    intr.h < 0 && (intr.h = -intr.h)  # as the reference leaves it (Integrator.jl:228-229)
     return
 end
 

@@ -263,6 +263,16 @@ def test_plain_integration_steps_and_default():
         O.integrate_nsteps(so, h, N)
         assert s.t[0] == so.t[0]
         P.check_state(s, so)
+    # a negative Integrator step with N > 0 takes the same backward steps as N < 0, and both calls leave
+    # intr.h positive (Integrator.jl:215-229)
+    s3, s4 = nbg.State(ic), nbg.State(ic)
+    i3, i4 = nbg.Integrator(nbg.ahl21, -h, 0.0, 100.0), nbg.Integrator(nbg.ahl21, h, 0.0, 100.0)
+    i3(s3, 20)
+    i4(s4, -20)
+    assert i3.h == h and i4.h == h
+    assert s3.t[0] < 0.0
+    for k in ("x", "v", "jac_step", "dqdt", "t"):
+        assert np.array_equal(getattr(s3, k), getattr(s4, k)), k
     s = nbg.State(ic)
     s2 = nbg.State(ic)
     intr = nbg.Integrator(nbg.ahl21, h, 0.0, 12.25)
