@@ -18,11 +18,13 @@
  *   - Body indices are 0-based in this ABI (the Julia shim passes ti - 1).
  *   - Return value: 0 on success, a negative NBG_E* code on failure; the
  *     message is available from nbg_last_error() on the calling thread.
- *   - The library never keeps a caller pointer after a call returns.
- *   - A context owns its CUDA streams (one, plus two more while the
- *     overlapped chunk pipeline is on) and its device buffers; calls on one
- *     context must not overlap.  Different contexts may be used from
- *     different threads.
+ *   - The library never keeps a caller pointer after a call returns, except
+ *     the arrays given to nbg_batch_submit, which the batch uses until
+ *     nbg_batch_wait has returned its run's result.
+ *   - A context owns its CUDA streams (one, plus three per group of systems
+ *     while the overlapped chunk pipeline is on) and its device buffers;
+ *     calls on one context must not overlap.  Different contexts may be used
+ *     from different threads.
  */
 #ifndef NBG_H
 #define NBG_H
@@ -178,6 +180,35 @@ int nbg_batch_integrate_transits(nbg_context* ctx, int nsys, const nbg_system_de
                                  double* v, const double* m, double* xerror, double* verror, double* jac_step,
                                  double* jac_error, double* dqdt, const uint8_t* pair, const double* jac_init,
                                  double* tt, double* dtdq0, double* dtdelements, int64_t* count, uint32_t* status);
+
+/*
+ * Asynchronous batch: nbg_batch_integrate_transits in steps, so that the
+ * caller's thread is free while a batch runs.  No reference counterpart (the
+ * reference integrates one system per call on the caller's thread).
+ *   nbg_batch_create   checks and copies nsys descriptors; binds the batch to
+ *                      ctx.
+ *   nbg_batch_submit   records the caller's packed host arrays (the arguments
+ *                      of nbg_batch_integrate_transits after desc, same
+ *                      layout and rules); nothing runs yet.
+ *   nbg_batch_run      starts nbg_batch_integrate_transits on a library host
+ *                      thread and returns at once.  Until nbg_batch_wait has
+ *                      returned the run's result, the arrays belong to the
+ *                      batch and ctx takes no other call.
+ *   nbg_batch_wait     waits up to timeout_ms (< 0: no limit); NBG_ETIMEOUT
+ *                      while the run continues, else the run's result, with
+ *                      its message from nbg_last_error on the waiting thread.
+ *   nbg_batch_destroy  waits for a started run, then frees the batch.
+ * After nbg_batch_wait has returned the result, the batch may be submitted
+ * (new arrays or the same) and run again.
+ */
+typedef struct nbg_batch nbg_batch;
+int nbg_batch_create(nbg_context* ctx, int nsys, const nbg_system_desc* desc, nbg_batch** out);
+int nbg_batch_submit(nbg_batch* b, double* t, double* x, double* v, const double* m, double* xerror, double* verror,
+                     double* jac_step, double* jac_error, double* dqdt, const uint8_t* pair, const double* jac_init,
+                     double* tt, double* dtdq0, double* dtdelements, int64_t* count, uint32_t* status);
+int nbg_batch_run(nbg_batch* b);
+int nbg_batch_wait(nbg_batch* b, int32_t timeout_ms);
+int nbg_batch_destroy(nbg_batch* b);
 
 /*
  * nbg_integrate_transit_parameters for nsys systems in one plan (arguments

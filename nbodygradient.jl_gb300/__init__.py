@@ -347,6 +347,48 @@ class Batch:
             p(self.status, _lib._U32)))
         return self
 
+    def start(self, ctx=None):
+        """nbg_batch_create / submit / run: the same integration as run(), on a library thread; returns at once.
+        The packed arrays belong to the run until wait() has returned."""
+        import ctypes
+        if getattr(self, "_async", None) is not None:
+            raise NbgError(_lib.NBG_EINVAL, "this batch is already running (wait() first)")
+        ctx = ctx or default_context()
+        L = _lib.load()
+        p = _lib.ptr
+        a = self.arrays
+        h = ctypes.c_void_p()
+        _lib.check(L.nbg_batch_create(ctx.handle, self.nsys, self.descriptors(), ctypes.byref(h)))
+        rc = L.nbg_batch_submit(
+            h, p(a["t"]), p(a["x"]), p(a["v"]), p(a["m"]), p(a["xerror"]), p(a["verror"]), p(a["jac_step"]),
+            p(a["jac_error"]), p(a["dqdt"]), p(a["pair"], _lib._U8), p(a["jac_init"]), p(a["tt"]), p(a["dtdq0"]),
+            p(a["dtdelements"]), p(a["count"], _lib._I64), p(self.status, _lib._U32))
+        if rc == _lib.NBG_OK:
+            rc = L.nbg_batch_run(h)
+        if rc != _lib.NBG_OK:
+            err = NbgError(rc, _lib.last_error())
+            L.nbg_batch_destroy(h)
+            raise err
+        self._async = (h, ctx)
+        return self
+
+    def wait(self, timeout_ms=-1):
+        """nbg_batch_wait for a run started by start(); raises NbgError (code NBG_ETIMEOUT) while it continues.
+        Once the run has ended, its batch handle is destroyed and its error, if any, raised."""
+        if getattr(self, "_async", None) is None:
+            raise NbgError(_lib.NBG_EINVAL, "no run in progress (start() first)")
+        L = _lib.load()
+        h = self._async[0]
+        rc = L.nbg_batch_wait(h, int(timeout_ms))
+        if rc == _lib.NBG_ETIMEOUT:
+            _lib.check(rc)
+        err = NbgError(rc, _lib.last_error()) if rc != _lib.NBG_OK else None
+        L.nbg_batch_destroy(h)
+        self._async = None
+        if err is not None:
+            raise err
+        return self
+
     def run_device(self, dev_arrays, ctx=None):
         """nbg_batch_integrate_transits_device on device buffers (a dict of torch CUDA tensors)."""
         ctx = ctx or default_context()

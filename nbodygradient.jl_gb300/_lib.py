@@ -38,7 +38,8 @@ EXPORTS = (
     "nbg_integrate_transit_parameters", "nbg_batch_integrate_transit_parameters",
     "nbg_batch_init_nbody", "nbg_batch_init_nbody_device", "nbg_integrate_cartesian", "nbg_autotune_device",
     "nbg_server_start", "nbg_server_enqueue", "nbg_server_wait_any", "nbg_server_poll", "nbg_server_stats",
-    "nbg_server_stop",
+    "nbg_server_stop", "nbg_batch_create", "nbg_batch_submit", "nbg_batch_run", "nbg_batch_wait",
+    "nbg_batch_destroy",
 )
 
 
@@ -154,6 +155,11 @@ def load(build_if_missing=True):
                                   _I64, ctypes.POINTER(RequestInfo)]
     L.nbg_server_stats.argtypes = [_VP, ctypes.POINTER(ServerStats)]
     L.nbg_server_stop.argtypes = [_VP]
+    L.nbg_batch_create.argtypes = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc), ctypes.POINTER(_VP)]
+    L.nbg_batch_submit.argtypes = [_VP, _D, _D, _D, _D, _D, _D, _D, _D, _D, _U8, _D, _D, _D, _D, _I64, _U32]
+    L.nbg_batch_run.argtypes = [_VP]
+    L.nbg_batch_wait.argtypes = [_VP, ctypes.c_int32]
+    L.nbg_batch_destroy.argtypes = [_VP]
     _lib = L
     return L
 

@@ -67,7 +67,8 @@ def build(force=False, verbose=False, jobs=None):
     units = [(os.path.join(CSRC, "nbg_cuda.cu"), os.path.join(BUILD_DIR, "nbg_cuda.o"), []),
              (os.path.join(CSRC, "nbg_noalloc.cu"), os.path.join(BUILD_DIR, "nbg_noalloc.o"), []),
              (os.path.join(CSRC, "nbg_server.cu"), os.path.join(BUILD_DIR, "nbg_server.o"), []),
-             (os.path.join(CSRC, "nbg_ics.cu"), os.path.join(BUILD_DIR, "nbg_ics.o"), [])]
+             (os.path.join(CSRC, "nbg_ics.cu"), os.path.join(BUILD_DIR, "nbg_ics.o"), []),
+             (os.path.join(CSRC, "nbg_batch_async.cu"), os.path.join(BUILD_DIR, "nbg_batch_async.o"), [])]
     for n in BODY_COUNTS:
         units.append((os.path.join(CSRC, "nbg_inst.cu"), os.path.join(BUILD_DIR, "nbg_inst_%d.o" % n),
                       ["-DNBG_N=%d" % n]))

@@ -103,3 +103,34 @@ def test_transit_parameters_and_cartesian_output_shapes():
 def test_server_start_fails_loudly_without_gpu():
     with pytest.raises(nbg.NbgError):
         nbg.Server()
+
+
+def test_async_batch_argument_and_order_checks_without_a_gpu():
+    """nbg_batch_*: NULL arguments, descriptor checks at create, and call-order errors (no run is started)."""
+    import ctypes
+    L = nbg._lib.load()
+    E, U, OK = nbg._lib.NBG_EINVAL, nbg._lib.NBG_EUNSUPPORTED, nbg._lib.NBG_OK
+    d = (nbg.SystemDesc * 2)()
+    for q in range(2):
+        d[q].n, d[q].ti, d[q].grad, d[q].ntt, d[q].h, d[q].tmax = 3, 0, 1, 10, 0.5, 10.0
+    h = ctypes.c_void_p()
+    assert L.nbg_batch_create(None, 2, d, ctypes.byref(h)) == E
+    assert L.nbg_batch_submit(None, *([None] * 16)) == E
+    assert L.nbg_batch_run(None) == E and L.nbg_batch_wait(None, 0) == E
+    assert L.nbg_batch_destroy(None) == OK
+    # create() stores the context pointer without using it, so its checks run without a GPU context
+    fake_ctx = ctypes.c_void_p(1)
+    assert L.nbg_batch_create(fake_ctx, 0, d, ctypes.byref(h)) == E
+    assert L.nbg_batch_create(fake_ctx, 2, d, None) == E
+    d[1].n = 11
+    assert L.nbg_batch_create(fake_ctx, 2, d, ctypes.byref(h)) == U
+    d[1].n, d[1].ti = 3, 3
+    assert L.nbg_batch_create(fake_ctx, 2, d, ctypes.byref(h)) == E
+    d[1].ti, d[1].h = 0, 0.0
+    assert L.nbg_batch_create(fake_ctx, 2, d, ctypes.byref(h)) == E
+    d[1].h = 0.5
+    assert L.nbg_batch_create(fake_ctx, 2, d, ctypes.byref(h)) == OK and h.value
+    assert L.nbg_batch_run(h) == E and "submitted" in nbg._lib.last_error()
+    assert L.nbg_batch_wait(h, 0) == E and "not running" in nbg._lib.last_error()
+    assert L.nbg_batch_submit(h, *([None] * 16)) == E
+    assert L.nbg_batch_destroy(h) == OK

@@ -191,6 +191,33 @@ def test_alone_and_in_batch_are_identical():
             assert np.array_equal(b.view(k, q), b1.view(k, 0)), (q, k)
 
 
+def test_async_batch_is_the_synchronous_call():
+    """nbg_batch_create / submit / run / wait (Batch.start / wait) gives the synchronous call's bits; a wait with
+    a zero limit either times out or returns the finished run."""
+    els, hs, tms = W.batch_uneven(16, seed=41, nmin=2, nmax=7)
+    specs = [(el, h, min(tm, 80.0), bool(q % 4)) for q, (el, h, tm) in enumerate(zip(els, hs, tms))]
+    states, timings, hs, tms, grads = _batch_inputs(specs)
+    bs, ba = [nbg.Batch([s.n for s in states], 0, hs, tms, [t.ntt for t in timings], grads) for _ in range(2)]
+    for q in range(len(states)):
+        bs.set_system(q, states[q], timings[q])
+        ba.set_system(q, states[q], timings[q])
+    bs.run()
+    ba.start()
+    try:
+        ba.wait(timeout_ms=0)
+        finished = True
+    except nbg.NbgError as e:
+        assert e.code == nbg._lib.NBG_ETIMEOUT
+        finished = False
+    if not finished:
+        ba.wait()
+    with pytest.raises(nbg.NbgError):
+        ba.wait()  # nothing left to wait for
+    for k in nbg.Batch.FIELDS:
+        assert np.array_equal(bs.arrays[k], ba.arrays[k]), k
+    assert np.array_equal(bs.status, ba.status)
+
+
 def test_batch_matches_oracle():
     els, hs, tms = W.batch_uneven(12, seed=31, nmin=2, nmax=9)
     specs = [(el, h, min(tm, 50.0), True) for el, h, tm in zip(els, hs, tms)]
