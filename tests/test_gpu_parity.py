@@ -218,6 +218,41 @@ def test_async_batch_is_the_synchronous_call():
     assert np.array_equal(bs.status, ba.status)
 
 
+def test_two_contexts_run_at_the_same_time():
+    """Two contexts integrate the same batch at the same time from two library threads (asynchronous batches);
+    each result is bitwise the batch run alone."""
+    els, hs, tms = W.batch_uneven(12, seed=43, nmin=2, nmax=6)
+    specs = [(el, h, min(tm, 60.0), True) for el, h, tm in zip(els, hs, tms)]
+    states, timings, hs, tms, grads = _batch_inputs(specs)
+
+    def make():
+        b = nbg.Batch([s.n for s in states], 0, hs, tms, [t.ntt for t in timings], grads)
+        for q in range(len(states)):
+            b.set_system(q, states[q], timings[q])
+        return b
+
+    ref = make().run()
+    c1, c2 = nbg.Context(0), nbg.Context(0)
+    b1, b2 = make(), make()
+    b1.start(c1)
+    try:
+        b2.start(c2)
+    except nbg.NbgError:
+        b1.wait()
+        raise
+    errs = []
+    for b in (b1, b2):  # both runs end before either context is closed
+        try:
+            b.wait()
+        except nbg.NbgError as e:
+            errs.append(e)
+    c1.close()
+    c2.close()
+    assert not errs, errs
+    for k in nbg.Batch.FIELDS:
+        assert np.array_equal(ref.arrays[k], b1.arrays[k]) and np.array_equal(ref.arrays[k], b2.arrays[k]), k
+
+
 def test_batch_matches_oracle():
     els, hs, tms = W.batch_uneven(12, seed=31, nmin=2, nmax=9)
     specs = [(el, h, min(tm, 50.0), True) for el, h, tm in zip(els, hs, tms)]
