@@ -29,13 +29,13 @@ os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 from . import _lib, build, workloads
 from ._lib import Context, NbgError, SystemDesc, default_context, device_info
-from .ics import CartesianIC, Elements, ElementsIC, hierarchy_nested, init_nbody, kepler_init
+from .ics import CartesianIC, Elements, ElementsIC, hierarchy, hierarchy_nested, init_nbody, kepler_init
 
 __all__ = ["Elements", "ElementsIC", "CartesianIC", "State", "TransitTiming", "TransitParameters", "CartesianOutput",
            "Integrator",
            "ahl21", "set_state",
            "Context", "NbgError", "default_context", "device_info", "integrate_transits_batch", "Batch", "Server",
-           "init_nbody_batch",
+           "init_nbody_batch", "hierarchy",
            "hierarchy_nested", "init_nbody", "kepler_init"]
 
 

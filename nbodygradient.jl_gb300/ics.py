@@ -6,7 +6,7 @@ same State):
   Elements            src/ics/InitialConditions.jl:21-107
   ElementsIC          src/ics/InitialConditions.jl:142-241
   CartesianIC         src/ics/InitialConditions.jl:259-282
-  hierarchy (nested)  src/ics/setup_hierarchy.jl:9-145 for H = [N, 1, ..., 1]
+  hierarchy           src/ics/setup_hierarchy.jl:9-179
   init_nbody          src/ics/init_nbody.jl:13-162
   kepler_init         src/ics/kepler_init.jl:66-210
   ekepler             src/ics/kepler.jl:1-41
@@ -15,6 +15,7 @@ rows (m, P, t0, e cos w, e sin w, I, Omega); x, v are 3 x N; jac_init is
 7N x 7N with per-body columns (P, t0, ecosw, esinw, I, Omega, m).
 """
 import math
+import os
 
 import numpy as np
 
@@ -22,16 +23,61 @@ GNEWT = 39.4845 / (365.242 * 365.242)  # src/NbodyGradient.jl:15
 THIRD = 1.0 / 3.0
 
 
+def _ieee_div(a, b):
+    """a / b with IEEE results for a zero divisor (Julia's Float64 division; Python raises instead)."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return float(np.float64(a) / np.float64(b))
+
+
+def _ieee_rem(a, b):
+    """Julia's a % b for Float64 (rem: the sign of a; NaN for b = 0, where math.fmod raises)."""
+    with np.errstate(invalid="ignore"):
+        return float(np.fmod(np.float64(a), np.float64(b)))
+
+
 class Elements:
-    """Orbital elements of one body (keyword constructor of InitialConditions.jl:64-107)."""
+    """Orbital elements of one body (InitialConditions.jl:21-107), with the reference's three constructors:
+
+      Elements(m, P, t0, ecosw, esinw, I, Omega)              e and w from ecosw, esinw; a = tp = 0; no checks
+      Elements(m, P, t0, ecosw, esinw, I, Omega, a, e, w, tp)  the eleven fields as given
+      Elements(m=..., P=..., ...)                              keywords, checked (the mass alone: a central body)
+
+    Keywords may also be spelled as the reference spells them (ecosω, esinω, Ω, ω).
+    """
 
     FIELDS = ("m", "P", "t0", "ecosw", "esinw", "I", "Omega")
+    ALL_FIELDS = ("m", "P", "t0", "ecosw", "esinw", "I", "Omega", "a", "e", "w", "tp")
+    _ALIASES = {"ecosω": "ecosw", "esinω": "esinw", "Ω": "Omega", "ω": "w"}
 
-    def __init__(self, m, P=math.nan, t0=math.nan, ecosw=math.nan, esinw=math.nan, I=math.nan, Omega=math.nan,
-                 a=math.nan, w=math.nan, e=math.nan, tp=math.nan):
+    def __init__(self, *args, **kw):
+        if args and kw:
+            raise TypeError("Elements takes positional fields or keywords, not both")
+        if args:
+            vals = [float(q) for q in args]
+            if len(vals) == 7:  # InitialConditions.jl:38-42
+                m, P, t0, ecosw, esinw, I, Omega = vals
+                vals += [0.0, math.sqrt(ecosw * ecosw + esinw * esinw), math.atan2(esinw, ecosw), 0.0]
+            elif len(vals) != 11:
+                raise TypeError("Elements takes 7 or 11 positional fields, got %d" % len(vals))
+            for f, q in zip(self.ALL_FIELDS, vals):
+                setattr(self, f, q)
+            return
+        kw = {self._ALIASES.get(k, k): v for k, v in kw.items()}
+        unknown = set(kw) - set(self.ALL_FIELDS)
+        if unknown:
+            raise TypeError("unknown Elements keyword(s): %s" % ", ".join(sorted(unknown)))
+        if "m" not in kw:
+            raise TypeError("Elements needs the keyword m")
+        self._from_keywords(**kw)
+
+    def _from_keywords(self, m, P=math.nan, t0=math.nan, ecosw=math.nan, esinw=math.nan, I=math.nan,
+                       Omega=math.nan, a=math.nan, w=math.nan, e=math.nan, tp=math.nan):
+        """The keyword constructor (InitialConditions.jl:64-107)."""
+        m, P, t0, ecosw, esinw, I, Omega, a, w, e, tp = (float(q) for q in (m, P, t0, ecosw, esinw, I, Omega, a, w,
+                                                                              e, tp))
         vals = [P, t0, ecosw, esinw, I, Omega, a, w, e, tp]
         if all(math.isnan(q) for q in vals):
-            self.m, self.P, self.t0, self.ecosw, self.esinw, self.I, self.Omega = float(m), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0
+            self.m, self.P, self.t0, self.ecosw, self.esinw, self.I, self.Omega = m, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0
             self.a = self.e = self.w = self.tp = 0.0
             return
         if math.isnan(P) and math.isnan(a):
@@ -64,14 +110,14 @@ class Elements:
             esinw = 0.0 if abs(esinw) < eps else esinw
             ecosw = 0.0 if abs(ecosw) < eps else ecosw
         t0 = 0.0 if math.isnan(t0) else t0
-        n = 2 * math.pi / P
+        n = _ieee_div(2 * math.pi, P)
         if math.isnan(tp) and e != 0:
-            tp = math.fmod(t0 - math.sqrt(1.0 - e * e) * ecosw / (n * (1.0 - esinw)) -
-                           (2.0 / n) * math.atan2(math.sqrt(1.0 - e) * (esinw + ecosw + e),
-                                                  math.sqrt(1.0 + e) * (esinw - ecosw - e)), P)
+            tp = _ieee_rem(t0 - _ieee_div(math.sqrt(1.0 - e * e) * ecosw, n * (1.0 - esinw)) -
+                           _ieee_div(2.0, n) * math.atan2(math.sqrt(1.0 - e) * (esinw + ecosw + e),
+                                                          math.sqrt(1.0 + e) * (esinw - ecosw - e)), P)
         elif math.isnan(tp):
-            tp = (math.pi / 2 + w) / n
-        self.m, self.P, self.t0, self.ecosw, self.esinw = float(m), P, t0, ecosw, esinw
+            tp = _ieee_div(math.pi / 2 + w, n)
+        self.m, self.P, self.t0, self.ecosw, self.esinw = m, P, t0, ecosw, esinw
         self.I = 0.0 if math.isnan(I) else I
         self.Omega = 0.0 if math.isnan(Omega) else Omega
         self.a = 0.0 if math.isnan(a) else a
@@ -89,6 +135,161 @@ def hierarchy_nested(N):
         H[i, i + 1] = 1.0
     H[N - 1, :] = -1.0
     return H
+
+
+class _Rows:
+    """Writes 1-based rows and inclusive column ranges of an N x N matrix, as the hierarchy builder's indexing
+    reads; an index outside the matrix is an invalid hierarchy (the reference stops with a BoundsError)."""
+
+    def __init__(self, n):
+        self.n = n
+        self.h = np.zeros((n, n))
+
+    def _check(self, r, c):
+        if not (1 <= r <= self.n and 1 <= c <= self.n):
+            raise ValueError("Invalid hierarchy: entry (%d, %d) outside the %d x %d matrix" % (r, c, self.n, self.n))
+
+    def put(self, r, c, val):
+        self._check(r, c)
+        self.h[r - 1, c - 1] = val
+
+    def fill(self, r, c1, c2, val):
+        """Columns c1..c2 of row r (none when c2 < c1)."""
+        if c2 < c1:
+            return
+        self._check(r, c1)
+        self._check(r, c2)
+        self.h[r - 1, c1 - 1:c2] = val
+
+
+def _whole(x):
+    """An integer-valued quotient (the reference converts it to Int64, which fails for a fraction)."""
+    if x != int(x):
+        raise ValueError("Invalid hierarchy: %g bodies do not split evenly" % x)
+    return int(x)
+
+
+def hierarchy(ic_vec):
+    """Hierarchy matrix from a hierarchy vector [N, b1, b2, ...], b_k binaries on level k (setup_hierarchy.jl:9-179).
+
+    The same level-filling rules and limits as the reference: the first level pairs bodies left to right, a
+    hierarchy with every body on the bottom level (2 b1 = N) or with more than one binary on its top level is
+    filled symmetrically, and any other fills one level after another, with at most two binaries on a level.
+    [N, 1, ..., 1] gives the fully nested matrix, [4, 2, 1] two binaries orbiting each other.
+    """
+    v = [int(q) for q in ic_vec]
+    if len(v) < 2:
+        raise ValueError("Invalid hierarchy: [N, binaries on level 1, ...] needs at least two entries")
+    nbody, bins = v[0], v[1:]
+    level = len(bins) if bins[-1] == 1 else len(bins) - 1
+    if not (bins[0] <= nbody / 2 and bins[0] <= 2 ** level):
+        raise ValueError("Invalid hierarchy.")
+    if sum(bins[:level]) != nbody - 1:
+        raise ValueError("Invalid hierarchy. Total # of binaries should = N-1")
+    w = _Rows(nbody)
+    # first level (setup_hierarchy.jl:34-62): binaries (1,2), (3,4), ... left to right
+    w.put(1, 1, -1.0)
+    w.put(1, 2, 1.0)
+    if bins[0] > 1:
+        j = 1 if bins[-1] == 1 else _whole(nbody / 2 - 1)
+        for i in range(1, bins[0]):
+            if j + 3 <= nbody:
+                w.put(i + 1, j + 2, -1.0)
+                w.put(i + 1, j + 3, 1.0)
+                j += 2
+    binsp, row, bodies = bins[0], bins[0] + 1, 2 * bins[0]
+    if bins[-1] > 1:
+        _hierarchy_symmetric_nest(w, nbody, row)
+    elif 2 * binsp == nbody:
+        _hierarchy_symmetric(w, nbody, binsp, row)
+    else:
+        _hierarchy_levels(w, nbody, bodies, bins, binsp, row)
+    w.h[nbody - 1, :] = -1.0
+    return w.h
+
+
+def _hierarchy_levels(w, nbody, bodies, bins, binsp, row):
+    """Levels 2, 3, ... one after another (nlevel, setup_hierarchy.jl:71-145): `bodies` counts the bodies
+    placed so far, `binsp` the binaries of the previous level; filling stops where the rules have no case."""
+    it = 2
+    while it <= len(bins):
+        b = bins[it - 1]
+        if nbody != bodies:
+            if b == binsp:
+                bodies += b
+            elif b > binsp:
+                bodies += 2 * b - 1
+        elif row == nbody - 1:  # every body placed: the last row below the top joins the two halves
+            if bodies % 4 > 2:
+                w.fill(row, 1, row - 2, -1.0)
+                w.fill(row, row - 1, bodies, 1.0)
+            else:
+                w.fill(row, 1, row - 1, -1.0)
+                w.fill(row, row, bodies, 1.0)
+            return
+        if nbody < bodies:
+            return
+        if binsp == 1 and b == 1:
+            w.fill(row, 1, bodies - binsp, -1.0)
+            w.fill(row, bodies - binsp + 1, bodies, 1.0)
+            row += binsp
+        elif binsp == 1 and b == 2:
+            w.fill(row, 1, bodies - 2 * binsp - 1, -1.0)
+            w.put(row, bodies - 2 * binsp, 1.0)
+            w.put(row + 1, bodies - 2 * binsp + 1, -1.0)
+            w.put(row + 1, bodies, 1.0)
+            row += 2
+        elif binsp == 2 and b == 1:
+            w.fill(row, 1, row - 1, -1.0)
+            w.fill(row, row, bodies, 1.0)
+            row += 1
+        elif binsp == 2 and b == 2:
+            w.fill(row, 1, row - 1, -1.0)
+            w.fill(row, row, bodies - 2 * (binsp - 1), 1.0)
+            w.put(row + 1, bodies - 2 * (binsp - 1) + 1, -1.0)
+            w.put(row + 1, bodies, 1.0)
+            row += 2
+        elif binsp == 3 and b == 2:
+            half, third = _whole(bodies / 2), _whole(bodies / 3)
+            w.fill(row, 1, half - 1, -1.0)
+            w.fill(row, half, 2 * third, 1.0)
+            w.fill(row + 1, 2 * third + 1, bodies, -1.0)
+            w.put(row + 1, bodies + 1, 1.0)
+            row += 2
+            bodies += 1
+        else:
+            return
+        binsp = b
+        it += 1
+
+
+def _hierarchy_symmetric(w, nbody, binsp, row):
+    """Every body on the bottom level (symmetric, setup_hierarchy.jl:151-164): pairs of binaries join four
+    bodies at a time, then the top row splits the system after its first binsp bodies."""
+    j = 0
+    while row < nbody - 1:
+        w.fill(row, 1 + j, 2 + j, -1.0)
+        w.fill(row, j + 3, j + 4, 1.0)
+        j += 4
+        row += 1
+    w.fill(row, 1, binsp, -1.0)
+    w.fill(row, binsp + 1, nbody, 1.0)
+
+
+def _hierarchy_symmetric_nest(w, nbody, row):
+    """More than one binary on the top level (symmetric_nest, setup_hierarchy.jl:166-179): both halves grow
+    a nested sequence side by side, then the top row joins the halves."""
+    hlf = _whole(nbody / 2)
+    j = 0
+    while row < nbody - 1:
+        w.fill(row, 1, 2 + j, -1.0)
+        w.put(row, 3 + j, 1.0)
+        w.fill(row + 1, hlf + 1, hlf + 2 + j, -1.0)
+        w.put(row + 1, hlf + 3 + j, 1.0)
+        j += 1
+        row += 2
+    w.fill(row, 1, hlf, -1.0)
+    w.fill(row, hlf + 1, nbody, 1.0)
 
 
 def _sigma_m(m, i, j, H):
@@ -289,29 +490,42 @@ def init_nbody(elements, t0, H):
     return x, v, np.asfortranarray(jac)
 
 
+def _read_rows(path, comments):
+    """A comma-separated numeric file as a matrix (readdlm(path, ',') with or without '#' comment lines)."""
+    return np.loadtxt(path, delimiter=",", comments="#" if comments else None, ndmin=2)
+
+
 class ElementsIC:
     """Initial conditions from a hierarchy and orbital elements (InitialConditions.jl:142-241).
 
-    H may be an int N (fully nested), a hierarchy matrix, or a list
-    [N, 1, ..., 1] (fully nested).  elements is an N x 7 array or a list of
-    Elements (one per body, in hierarchy order).
+    H may be an int N (fully nested), a hierarchy vector [N, b1, b2, ...]
+    (hierarchy()), or a hierarchy matrix.  elements is an N x 7 array (more
+    rows are allowed; the first N are used), a list of Elements (one per body,
+    in hierarchy order, missing bodies zero), or the name of a comma-separated
+    file with '#' comment lines.
     """
 
     def __init__(self, t0, H, *elements, der=True):
-        if len(elements) == 1 and not isinstance(elements[0], Elements):
+        if isinstance(H, (int, np.integer)):
+            Hm = hierarchy_nested(int(H))
+        else:
+            Ha = np.asarray(H)
+            if Ha.ndim == 1:
+                Hm = hierarchy([int(q) for q in Ha])
+            elif Ha.ndim == 2:
+                Hm = np.array(Ha, dtype=np.float64)
+            else:
+                raise ValueError("H must be a body count, a hierarchy vector or a hierarchy matrix")
+        nbody = Hm.shape[0]
+        if len(elements) == 1 and isinstance(elements[0], (str, os.PathLike)):
+            el = _read_rows(elements[0], comments=True)
+        elif len(elements) == 1 and not isinstance(elements[0], (Elements, list, tuple)):
             el = np.array(elements[0], dtype=np.float64)
         else:
             els = elements[0] if (len(elements) == 1 and isinstance(elements[0], (list, tuple))) else elements
-            el = np.array([e.row() for e in els], dtype=np.float64)
-        if isinstance(H, (int, np.integer)):
-            Hm = hierarchy_nested(int(H))
-        elif isinstance(H, (list, tuple)) and all(int(q) == 1 for q in H[1:]):
-            Hm = hierarchy_nested(int(H[0]))
-        else:
-            Hm = np.array(H, dtype=np.float64)
-            if Hm.ndim != 2:
-                raise ValueError("only fully nested hierarchy vectors or explicit hierarchy matrices are supported")
-        nbody = Hm.shape[0]
+            el = np.zeros((nbody, 7))
+            for i, e in enumerate(els):  # InitialConditions.jl:213-220: unlisted bodies stay zero
+                el[i] = e.row()
         self.elements = np.array(el[:nbody, :], dtype=np.float64)
         self.H = Hm
         self.nbody = nbody
@@ -325,10 +539,14 @@ class ElementsIC:
 
 
 class CartesianIC:
-    """Initial conditions from Cartesian coordinates (InitialConditions.jl:259-282)."""
+    """Initial conditions from Cartesian coordinates (InitialConditions.jl:259-282): rows (m, x, y, z, vx, vy,
+    vz), as a matrix or the name of a comma-separated file (read without comment lines, as the reference)."""
 
     def __init__(self, t0, N, coords):
-        c = np.array(coords, dtype=np.float64)
+        if isinstance(coords, (str, os.PathLike)):
+            c = _read_rows(coords, comments=False)
+        else:
+            c = np.array(coords, dtype=np.float64)
         self.m = c[:N, 0].copy()
         self.x = np.asfortranarray(c[:N, 1:4].T)
         self.v = np.asfortranarray(c[:N, 4:7].T)
