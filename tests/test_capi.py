@@ -36,12 +36,14 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(L, f)
 
 
-def test_built_for_sm_103a():
-    path = nbg.build.build()
-    out = subprocess.run(["cuobjdump", "--list-elf", path], capture_output=True, text=True)
-    if out.returncode != 0:
-        pytest.skip("cuobjdump not available")
-    assert "sm_103a" in out.stdout
+def test_built_for_sm_103a_only():
+    """Every unit compiles for exactly one target, sm_103a (no PTX for other architectures, no JIT), with
+    separately rounded products (--fmad=false) and no host FP contraction."""
+    flags = nbg.build.NVCC_FLAGS
+    gencodes = [flags[i + 1] for i, f in enumerate(flags) if f == "-gencode"]
+    assert gencodes == ["arch=compute_103a,code=sm_103a"]
+    assert not any(f.startswith(("-arch", "--gpu-architecture", "-code")) for f in flags)
+    assert "--fmad=false" in flags and "-ffp-contract=off" in flags
 
 
 def test_version_and_error_buffer():
