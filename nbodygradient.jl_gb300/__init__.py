@@ -33,7 +33,7 @@ from .ics import CartesianIC, Elements, ElementsIC, hierarchy, hierarchy_nested,
 
 __all__ = ["Elements", "ElementsIC", "CartesianIC", "State", "TransitTiming", "TransitParameters", "CartesianOutput",
            "Integrator",
-           "ahl21", "set_state",
+           "ahl21", "set_state", "initialize", "dState", "Derivatives",
            "Context", "NbgError", "default_context", "device_info", "integrate_transits_batch", "Batch", "Server",
            "init_nbody_batch", "hierarchy",
            "hierarchy_nested", "init_nbody", "kepler_init"]
@@ -73,6 +73,33 @@ class State:
 
     def isfinite(self):
         return bool(np.all(np.isfinite(self.x)) and np.all(np.isfinite(self.v)) and np.all(np.isfinite(self.jac_step)))
+
+
+class Derivatives:
+    """The reference's preallocated step scratch (src/PreAllocArrays.jl:65-113), as taken by the three-argument
+    intr(s, tt, d; grad) (Transits.jl:140).  The GPU path keeps its scratch on the device, so this holds the
+    body count only.  Derivatives(n) or, as in Julia, Derivatives(T, n)."""
+
+    def __init__(self, *args):
+        if len(args) not in (1, 2):
+            raise TypeError("Derivatives(n) or Derivatives(T, n)")
+        self.n = int(args[-1])
+
+
+def dState(ic):
+    """State(ic) and a Derivatives for it (src/integrator/Integrator.jl:106-110)."""
+    return State(ic), Derivatives(ic.nbody)
+
+
+def initialize(s, ic):
+    """initialize! (src/integrator/Integrator.jl:112-121): x, v and jac_init from ic, zero Kahan errors; the
+    other State fields are kept."""
+    x, v, jac_init = ic.init_nbody()
+    s.x[...] = x
+    s.v[...] = v
+    s.jac_init[...] = jac_init
+    s.xerror[...] = 0.0
+    s.verror[...] = 0.0
 
 
 def set_state(s_old, s_new):
@@ -198,11 +225,23 @@ class Integrator:
         self.scheme = scheme
         self.h, self.t0, self.tmax = float(h), float(t0), float(tmax)
 
-    def __call__(self, s, tt=None, grad=True, ctx=None):
-        """intr(s, tt::TransitTiming; grad)   Transits.jl:173  (transit times)
+    def __call__(self, s, tt=None, d=None, *, grad=True, return_arrays=False, ctx=None):
+        """intr(s, tt::TransitTiming; grad)   Transits.jl:173  (transit times; also TransitParameters)
+        intr(s, tt, d::Derivatives; grad)   Transits.jl:140  (the same with preallocated scratch, e.g. dState)
         intr(s, time::float; grad)          Integrator.jl:159 (integrate to time)
         intr(s, N::int; grad)               Integrator.jl:210 (N steps)
-        intr(s; grad)                       Integrator.jl:247 (to s.t + tmax)"""
+        intr(s; grad)                       Integrator.jl:247 (to s.t + tmax)
+        intr(s, o::CartesianOutput)         Outputs.jl:26
+
+        grad is keyword-only, as in the reference.  return_arrays=True returns None: the step scratch the
+        reference would hand back lives on the device."""
+        if d is not None:
+            if not isinstance(d, Derivatives):
+                raise TypeError("the third argument of intr(s, tt, d) is a Derivatives (dState(ic) makes one)")
+            if not isinstance(tt, (TransitTiming, TransitParameters)):
+                raise TypeError("intr(s, tt, d) takes a TransitTiming or TransitParameters")
+            if d.n != s.n:
+                raise ValueError("Derivatives for %d bodies, State for %d" % (d.n, s.n))
         ctx = ctx or default_context()
         L = _lib.load()
         p = _lib.ptr

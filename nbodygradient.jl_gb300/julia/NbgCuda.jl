@@ -5,6 +5,7 @@
 # than the reference's, for Float64 states and the ahl21! scheme:
 #   intr(s, tt::TransitTiming; grad)        (src/transits/Transits.jl:173-180)
 #   intr(s, ttbv::TransitParameters; grad)  (same, TransitParameters output)
+#   intr(s, tt, d::Derivatives; grad)       (src/transits/Transits.jl:140, both outputs)
 #   intr(s, time::Float64; grad)            (src/integrator/Integrator.jl:159)
 #   intr(s, N::Int64; grad)                 (src/integrator/Integrator.jl:210)
 #   intr(s, o::CartesianOutput)             (src/outputs/Outputs.jl:26)
@@ -72,6 +73,19 @@ function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, ttbv::Tra
     end
     rc == 0 || error("libnbg_cuda: ", last_error())
     return nothing
+end
+
+# The three-argument forms with preallocated Derivatives (Transits.jl:140,
+# e.g. after dState(ic)) take the same GPU path; the scratch lives on the
+# device, so d is not used.
+function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, tt::TransitTiming{Float64},
+                                                    d::NbodyGradient.Derivatives{Float64}; grad::Bool=true)
+    return intr(s, tt; grad=grad)
+end
+
+function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, ttbv::TransitParameters{Float64},
+                                                    d::NbodyGradient.Derivatives{Float64}; grad::Bool=true)
+    return intr(s, ttbv; grad=grad)
 end
 
 # ccall's argument types must be a literal tuple, so the State pointers

@@ -5,6 +5,7 @@ import os
 import re
 import subprocess
 
+import numpy as np
 import pytest
 
 import nbg
@@ -136,3 +137,28 @@ def test_async_batch_argument_and_order_checks_without_a_gpu():
     assert L.nbg_batch_wait(h, 0) == E and "not running" in nbg._lib.last_error()
     assert L.nbg_batch_submit(h, *([None] * 16)) == E
     assert L.nbg_batch_destroy(h) == OK
+
+
+def test_derivatives_dstate_and_initialize_without_a_gpu():
+    """dState / Derivatives / initialize (Integrator.jl:106-121) and the argument checks of intr(s, tt, d)."""
+    from nbg import workloads as W
+    el, h, _ = W.plain_3body(0)
+    ic = W.ic_of(el)
+    s, d = nbg.dState(ic)
+    assert isinstance(d, nbg.Derivatives) and d.n == 3 and nbg.Derivatives(np.float64, 3).n == 3
+    x0 = s.x.copy()
+    s.x[...] += 1.0
+    s.xerror[...] = 1e-20
+    s.jac_init[...] = 0.0
+    nbg.initialize(s, ic)
+    assert np.array_equal(s.x, x0) and not s.xerror.any() and np.array_equal(s.jac_init, nbg.State(ic).jac_init)
+    intr = nbg.Integrator(nbg.ahl21, h, 0.0, 10.0)
+    tt = nbg.TransitTiming(10.0, ic)
+    with pytest.raises(TypeError):
+        intr(s, tt, object())
+    with pytest.raises(TypeError):
+        intr(s, 5.0, d)
+    with pytest.raises(ValueError):
+        intr(s, tt, nbg.Derivatives(4))
+    with pytest.raises(TypeError):
+        intr(s, tt, d, True)  # grad is keyword-only

@@ -132,6 +132,23 @@ def test_second_call_continues_counts():
     compare(s, tt, so, to, 400.0)
 
 
+def test_three_argument_call_with_dstate():
+    """s, d = dState(ic); intr(s, tt, d; grad) (Transits.jl:140) gives the bits of intr(s, tt; grad)."""
+    el, h, _ = W.plain_3body(8)
+    ic = nbg.ElementsIC(0.0, 3, el)
+    s1, d = nbg.dState(ic)
+    s2 = nbg.State(ic)
+    t1, t2 = nbg.TransitTiming(150.0, ic), nbg.TransitTiming(150.0, ic)
+    intr = nbg.Integrator(nbg.ahl21, h, 0.0, 150.0)
+    assert intr(s1, t1, d, grad=True) is None
+    intr(s2, t2, grad=True)
+    for k in ("x", "v", "jac_step", "dqdt", "t"):
+        assert np.array_equal(getattr(s1, k), getattr(s2, k)), k
+    for k in ("tt", "dtdq0", "dtdelements", "count"):
+        assert np.array_equal(getattr(t1, k), getattr(t2, k)), k
+    assert t1.count.sum() > 0
+
+
 def test_ntt_overflow_counts_and_drops():
     """Transits beyond ntt are counted but not stored (timing.jl:18-19)."""
     el, h, tmax = W.plain_3body(8)
