@@ -85,21 +85,22 @@ def test_hierarchy_vectors():
 
 
 def test_double_binary_ics_match_oracle():
-    """init_nbody for the hierarchy [4, 2, 1] (two binaries orbiting each other) against the oracle."""
-    el = np.array([[1.0, 0, 0, 0, 0, 0, 0],
-                   [0.8, 10.0, 2.0, 0.01, 0.02, np.pi / 2, 0.0],
-                   [0.5, 0.0, 0, 0, 0, 0, 0],
-                   [0.3, 12.0, 5.0, -0.02, 0.01, np.pi / 2, 0.1]])
-    # elements rows of the Keplerians (init_nbody.jl): row k + 1 describes row k of H
-    el_k = np.array([el[0], el[1], el[3], [0.0, 400.0, 100.0, 0.05, 0.0, np.pi / 2, 0.0]])
-    el_k[3, 0] = el[2, 0]
+    """init_nbody for the hierarchy [4, 2, 1] (two binaries orbiting each other) against the oracle.  Row r of
+    the elements holds body r's mass; the orbits go to the Keplerians as kepcalc assigns them (init_nbody.jl:
+    60-95): a-b takes row 2, c-d (a new branch) row 4, the outer orbit row 3."""
+    el = np.array([[1.0, 0, 0, 0, 0, 0, 0],                                  # body a
+                   [0.8, 10.0, 2.0, 0.01, 0.02, np.pi / 2, 0.0],              # body b; orbit a-b
+                   [0.5, 400.0, 100.0, 0.05, 0.0, np.pi / 2, 0.0],            # body c; orbit (ab)-(cd)
+                   [0.3, 12.0, 5.0, -0.02, 0.01, np.pi / 2, 0.1]])            # body d; orbit c-d
     H = nbg.hierarchy([4, 2, 1])
-    ic = nbg.ElementsIC(0.0, [4, 2, 1], el_k)
+    ic = nbg.ElementsIC(0.0, [4, 2, 1], el)
     assert np.array_equal(ic.H, H)
     x, v, j = ic.init_nbody()
-    xo, vo, jo = O.init_nbody(el_k, 0.0, H)
+    xo, vo, jo = O.init_nbody(el, 0.0, H)
+    # the binaries are tight and the outer orbit wide: |c - d| is the 12-day separation, not the 400-day one
+    assert np.linalg.norm(x[:, 2] - x[:, 3]) < 0.2 * np.linalg.norm(x[:, :2].mean(axis=1) - x[:, 2:].mean(axis=1))
     assert _rel(x, xo) < 1e-13 and _rel(v, vo) < 1e-13 and _rel(j, jo) < 1e-12
-    assert abs(float((x * ic.m).sum(axis=1).max())) < 1e-12 * float(np.abs(x).max())  # centre of mass at rest
+    assert float(np.abs((x * ic.m).sum(axis=1)).max()) < 1e-12 * float(np.abs(x).max())  # centre of mass at 0
 
 
 REF_COORDINATES = os.path.join(os.path.dirname(REF_ELEMENTS), "coordinates.txt")

@@ -304,3 +304,41 @@ def test_init_nbody_jacobian_synthetic():
     _, _, jac = O.init_nbody(els[0], 0.0)
     num = O.fd_init_nbody(els[0], 0.0, [1e-10] * 6 + [1e-13], dq_star_mass=1e-15)
     assert close(jac, num)
+
+
+def keplerian_element_rows(H):
+    """The elements row each Keplerian (row i < N - 1 of H) takes in kepcalc (init_nbody.jl:60-95): i + 1,
+    shifted by one row after next for a Keplerian that starts a new branch (its H row is zero on body 1)."""
+    rows, b = [], 0
+    for i in range(H.shape[0] - 1):
+        if H[i, 0] == 0:
+            b += 1
+        rows.append(i + 1 + b)
+        if b > 0:
+            b -= 2
+        elif b < 0:
+            b = 0
+    return rows
+
+
+def test_init_nbody_jacobian_double_binary():
+    """jac_init for the hierarchy [4, 2, 1] (two binaries orbiting each other; the inverse A-matrix and its mass
+    derivatives are no longer those of nested Jacobi coordinates) against two-sided quad differences.
+    jac_init's element columns are per Keplerian (block i + 1 for row i of H, init_nbody.jl:84-86), the
+    Keplerians take elements rows 1, 3, 2 here (the outer orbit is row 2), and the mass columns are per body;
+    the differences perturb element row r into block r, so the orbital blocks are compared through that map."""
+    import nbg
+    H = nbg.hierarchy([4, 2, 1])
+    el = np.array([[1.0, 0, 0, 0, 0, 0, 0],                                  # body a
+                   [0.8, 10.0, 2.0, 0.01, 0.02, np.pi / 2, 0.0],              # body b; orbit a-b
+                   [0.5, 400.0, 100.0, 0.05, 0.03, np.pi / 2 + 0.02, 0.0],    # body c; orbit (ab)-(cd)
+                   [0.3, 12.0, 5.0, -0.02, 0.01, np.pi / 2 - 0.01, 0.1]])     # body d; orbit c-d
+    rows = keplerian_element_rows(H)
+    assert rows == [1, 3, 2]
+    _, _, jac = O.init_nbody(el, 0.0, H)
+    num = O.fd_init_nbody(el, 0.0, [1e-10] * 6 + [1e-12], dq_star_mass=1e-15, H=H)
+    mapped = num.copy()
+    for i, r in enumerate(rows):
+        mapped[:, 7 * (i + 1):7 * (i + 1) + 6] = num[:, 7 * r:7 * r + 6]
+    assert close(jac, mapped)
+    assert not close(jac, num)  # the row-by-row layout differs for this hierarchy
