@@ -428,6 +428,14 @@ class Batch:
             raise err
         return self
 
+    def __del__(self):
+        # a run in progress writes into this batch's arrays: it ends before they are released
+        if getattr(self, "_async", None) is not None:
+            try:
+                self.wait()
+            except Exception:
+                pass
+
     def run_device(self, dev_arrays, ctx=None):
         """nbg_batch_integrate_transits_device on device buffers (a dict of torch CUDA tensors)."""
         ctx = ctx or default_context()
