@@ -61,10 +61,13 @@ typedef struct nbg_context nbg_context;
 int nbg_create(int device, nbg_context** out);
 int nbg_destroy(nbg_context* ctx);
 
-/* Copy the calling thread's last error message into buf (NUL-terminated). */
+/* Copy the calling thread's last error message into buf (NUL-terminated).
+ * No reference counterpart (the reference throws Julia exceptions; the shim
+ * turns a non-zero return code into error(...) with this message). */
 int nbg_last_error(char* buf, size_t len);
 
-/* Library version (major * 10000 + minor * 100 + patch). */
+/* Library version (major * 10000 + minor * 100 + patch) and device facts
+ * (no reference counterpart). */
 int nbg_version(void);
 
 typedef struct {
@@ -377,13 +380,14 @@ int nbg_server_stats(nbg_server* srv, nbg_server_stats_t* out);
 /* Cancel requests not yet admitted, finish the running ones, free the server. */
 int nbg_server_stop(nbg_server* srv);
 
-/* Tuning knobs of a context.  Results do not depend on them.
+/* Tuning knobs of a context (no reference counterpart).  Results do not
+ * depend on them.
  * chunk_steps: integration steps per producer/consumer chunk (default 64,
  *   shortened for batches whose per-chunk operator records would pass
  *   4 GiB; 0 keeps the current value);
  * overlap: 1 (default) runs the orbit producer on its own stream one chunk
  *   ahead of the transit searches, operator kernels and Jacobian consumer
- *   (two more streams of the context); 0 runs everything on one stream;
+ *   (three streams per group of systems); 0 runs everything on one stream;
  *   a negative value keeps the current setting. */
 int nbg_set_tuning(nbg_context* ctx, int chunk_steps, int overlap);
 
@@ -443,7 +447,8 @@ int nbg_set_orbit_team(nbg_context* ctx, int mode);
  * latency-bound producer.  Default 1, 0, 0. */
 int nbg_set_producer_layout(nbg_context* ctx, int warps_per_block, int smem_kb, int guard_kb);
 
-/* Record an event pair around kernel launches (0: off, the default; 1: every
+/* Profiling (no reference counterpart).
+ * Record an event pair around kernel launches (0: off, the default; 1: every
  * orbit-producer, transit, operator and Jacobian launch; 2: the Jacobian
  * consumer's launches; 3: one consumer launch per group and call, its
  * middle chunk, with nbg_last_timing's jacobian_ms scaled to all the
@@ -451,7 +456,8 @@ int nbg_set_producer_layout(nbg_context* ctx, int warps_per_block, int smem_kb, 
  * pair per call perturbs them least). */
 int nbg_set_profiling(nbg_context* ctx, int on);
 
-/* Launch counts of the last call, per kernel kind. */
+/* Launch counts of the last call, per kernel kind (no reference
+ * counterpart; measurement helpers, as the two below). */
 int nbg_last_kernel_stats(nbg_context* ctx, int64_t* orbit_launches, int64_t* jacobian_launches);
 
 /* Number of kernels launched by the last call. */
