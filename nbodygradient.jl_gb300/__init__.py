@@ -386,13 +386,16 @@ class Batch:
             p(self.status, _lib._U32)))
         return self
 
-    def start(self, ctx=None):
+    def start(self, ctx=None, device=0):
         """nbg_batch_create / submit / run: the same integration as run(), on a library thread; returns at once.
-        The packed arrays belong to the run until wait() has returned."""
+        The packed arrays belong to the run until wait() has returned.  Without ctx the run gets a context of
+        its own on `device` (closed by wait()), so calls on the default context may go on meanwhile; a context
+        passed in takes no other call until wait() has returned."""
         import ctypes
         if getattr(self, "_async", None) is not None:
             raise NbgError(_lib.NBG_EINVAL, "this batch is already running (wait() first)")
-        ctx = ctx or default_context()
+        own = ctx is None
+        ctx = Context(device) if own else ctx
         L = _lib.load()
         p = _lib.ptr
         a = self.arrays
@@ -407,8 +410,10 @@ class Batch:
         if rc != _lib.NBG_OK:
             err = NbgError(rc, _lib.last_error())
             L.nbg_batch_destroy(h)
+            if own:
+                ctx.close()
             raise err
-        self._async = (h, ctx)
+        self._async = (h, ctx, own)
         return self
 
     def wait(self, timeout_ms=-1):
@@ -417,13 +422,15 @@ class Batch:
         if getattr(self, "_async", None) is None:
             raise NbgError(_lib.NBG_EINVAL, "no run in progress (start() first)")
         L = _lib.load()
-        h = self._async[0]
+        h, ctx, own = self._async
         rc = L.nbg_batch_wait(h, int(timeout_ms))
         if rc == _lib.NBG_ETIMEOUT:
             _lib.check(rc)
         err = NbgError(rc, _lib.last_error()) if rc != _lib.NBG_OK else None
         L.nbg_batch_destroy(h)
         self._async = None
+        if own:
+            ctx.close()
         if err is not None:
             raise err
         return self
