@@ -1173,17 +1173,16 @@ int nbg_create(int device, nbg_context** out) {
 int nbg_destroy(nbg_context* ctx) {
   if (!ctx) return NBG_OK;
   cudaSetDevice(ctx->device);
+  // every stream of the context is idle before its buffers are freed
   cudaStreamSynchronize(ctx->stream);
+  for (cudaStream_t s2 : ctx->gstreams) cudaStreamSynchronize(s2);
   for (auto& kv : ctx->pool)
     if (kv.second.p) cudaFree(kv.second.p);
   cudaEventDestroy(ctx->ev0);
   cudaEventDestroy(ctx->ev1);
   for (auto e : ctx->prof_events) cudaEventDestroy(e);
   for (auto e : ctx->sync_events) cudaEventDestroy(e);
-  for (cudaStream_t s2 : ctx->gstreams) {
-    cudaStreamSynchronize(s2);
-    cudaStreamDestroy(s2);
-  }
+  for (cudaStream_t s2 : ctx->gstreams) cudaStreamDestroy(s2);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return NBG_OK;
