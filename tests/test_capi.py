@@ -162,3 +162,26 @@ def test_derivatives_dstate_and_initialize_without_a_gpu():
         intr(s, tt, nbg.Derivatives(4))
     with pytest.raises(TypeError):
         intr(s, tt, d, True)  # grad is keyword-only
+
+
+def test_binding_argument_counts_match_the_header():
+    """Every ctypes binding declares as many arguments as the header's prototype, with a compatible kind
+    (integer, floating point or pointer) at each position."""
+    import test_julia_shim as S
+    protos = S.header_prototypes()
+    L = nbg._lib.load()
+    ints = {ctypes.c_int, ctypes.c_int32, ctypes.c_int64, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_uint64}
+    for name in nbg._lib.EXPORTS:
+        fn = getattr(L, name)
+        if fn.argtypes is None:
+            assert protos[name][1] == [], name  # nbg_version(void)
+            continue
+        ctypes_ = protos[name][1]
+        assert len(fn.argtypes) == len(ctypes_), (name, len(fn.argtypes), len(ctypes_))
+        for pos, (py, c) in enumerate(zip(fn.argtypes, ctypes_)):
+            if c.endswith("*"):
+                assert py is ctypes.c_void_p or py is ctypes.c_char_p or issubclass(py, ctypes._Pointer), (name, pos)
+            elif c == "double":
+                assert py is ctypes.c_double, (name, pos)
+            else:
+                assert py in ints, (name, pos, c)
