@@ -1712,6 +1712,7 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
     const double slope = (T2 > T1) ? (tms[1] - tms[0]) / (T2 - T1) : 0.0;
     const double ms = (T2 > T1) ? tms[0] + std::max(0.0, slope) * ((double)longest - T1) : tms[1];
     if (report && nrep < report_len) {
+      memset(&report[nrep], 0, sizeof(report[nrep]));
       report[nrep].chunk_steps = cd.chunk;
       report[nrep].orbit_team = cd.team;
       report[nrep].orbit_lanes = cd.spw;
