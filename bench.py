@@ -378,6 +378,8 @@ def main():
     ap.add_argument("--serve-chunk", type=int, default=32)
     ap.add_argument("--serve-tmax-max", type=float, default=0.0, help="cap on a request's tmax (0: none)")
     ap.add_argument("--serve-timeout", type=float, default=600.0)
+    ap.add_argument("--fp64-probe", action="store_true",
+                    help="print the measured FP64 rates (DFMA; DMMA alone; DMMA interleaved with DFMA), then exit")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -399,6 +401,15 @@ def main():
     torch.cuda.set_device(local_rank)
     if args.serve:
         run_serve(args, nbg)
+        return
+    if args.fp64_probe:
+        ctx = nbg.Context(local_rank)
+        dfma = ctx.fp64_peak_tflops()
+        mma, _ = ctx.fp64_mma_peak_tflops(False)
+        mixed, share = ctx.fp64_mma_peak_tflops(True)
+        print(json.dumps({"fp64_probe": {"dfma_tflops": dfma, "dmma_tflops": mma, "dmma_plus_dfma_tflops": mixed,
+                                         "dfma_share_of_mixed": share, "unit": "TFLOP/s (FMA = 2 flops)"}}),
+              flush=True)
         return
     ctx = nbg.Context(local_rank)
     if args.chunk or args.serial:

@@ -473,6 +473,16 @@ int nbg_last_host_time(nbg_context* ctx, double* enqueue_ms);
  * counterpart in the reference; a measurement helper. */
 int nbg_fp64_peak(nbg_context* ctx, double* tflops);
 
+/* Measured FP64 tensor-core throughput of the context's device (TFLOP/s, one
+ * mma.sync m8n8k4 f64 = 512 flops), after checking one exact product against
+ * the documented fragment layout (NBG_EUNSUPPORTED if it differs).  With
+ * with_dfma != 0 every DMMA is interleaved with 8 independent DFMAs of the
+ * same warp and *tflops counts both; *dfma_share (may be NULL) is the DFMA
+ * part of those flops.  Compared with nbg_fp64_peak this shows whether the
+ * tensor path adds FP64 throughput beside the FMA pipe.  No counterpart in
+ * the reference; a measurement helper. */
+int nbg_fp64_mma_peak(nbg_context* ctx, int with_dfma, double* tflops, double* dfma_share);
+
 #ifdef __cplusplus
 }
 #endif

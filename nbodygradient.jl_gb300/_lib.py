@@ -30,7 +30,7 @@ MAX_BODIES = 10
 EXPORTS = (
     "nbg_create", "nbg_destroy", "nbg_last_error", "nbg_version", "nbg_device_info",
     "nbg_integrate_transits", "nbg_batch_integrate_transits", "nbg_batch_integrate_transits_device",
-    "nbg_set_tuning", "nbg_last_timing", "nbg_last_launch_count", "nbg_fp64_peak",
+    "nbg_set_tuning", "nbg_last_timing", "nbg_last_launch_count", "nbg_fp64_peak", "nbg_fp64_mma_peak",
     "nbg_set_profiling", "nbg_last_kernel_stats", "nbg_set_orbit_lanes", "nbg_set_orbit_team",
     "nbg_set_producer_layout", "nbg_last_host_time",
     "nbg_batch_integrate_transits_noalloc",
@@ -141,6 +141,7 @@ def load(build_if_missing=True):
     L.nbg_last_launch_count.argtypes = [_VP]
     L.nbg_last_launch_count.restype = ctypes.c_int64
     L.nbg_fp64_peak.argtypes = [_VP, _D]
+    L.nbg_fp64_mma_peak.argtypes = [_VP, ctypes.c_int, _D, _D]
     L.nbg_set_profiling.argtypes = [_VP, ctypes.c_int]
     L.nbg_set_orbit_lanes.argtypes = [_VP, ctypes.c_int]
     L.nbg_set_orbit_team.argtypes = [_VP, ctypes.c_int]
@@ -250,6 +251,12 @@ class Context:
         v = ctypes.c_double()
         check(load().nbg_fp64_peak(self._h, ctypes.byref(v)))
         return v.value
+
+    def fp64_mma_peak_tflops(self, with_dfma=False):
+        """(TFLOP/s, DFMA share of those flops) of the FP64 tensor-core probe."""
+        v, sh = ctypes.c_double(), ctypes.c_double()
+        check(load().nbg_fp64_mma_peak(self._h, int(with_dfma), ctypes.byref(v), ctypes.byref(sh)))
+        return v.value, sh.value
 
 
 _default_ctx = None

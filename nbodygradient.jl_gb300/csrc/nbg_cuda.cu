@@ -1121,6 +1121,70 @@ __global__ void fp64_peak_kernel(double* out, int iters) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// FP64 tensor-core (DMMA) probes: mma.sync m8n8k4 with f64 operands, one
+// 8x4 by 4x8 product into an 8x8 accumulator per warp instruction (256 FMAs).
+// Fragments (PTX ISA, mma.m8n8k4 .f64): lane l holds A[l/4][l%4],
+// B[l%4][l/4] and C[l/4][2(l%4)], C[l/4][2(l%4)+1].
+__device__ __forceinline__ void dmma_8x8x4(double& c0, double& c1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+               : "+d"(c0), "+d"(c1)
+               : "d"(a), "d"(b));
+}
+
+// One product of exactly representable small operands: err[lane] = the
+// difference of this lane's two accumulator entries from the exact result
+// (0 when the fragment layout above holds).  One warp, 32 outputs.
+__global__ void fp64_mma_check_kernel(double* err) {
+  const int l = threadIdx.x & 31, g = l >> 2, t = l & 3;
+  auto A = [](int r, int k) { return (r + 1) + 0.5 * k; };
+  auto B = [](int k, int n) { return (k + 1) * (double)(n - 3); };
+  auto C = [](int r, int n) { return (double)(r * n); };
+  double c0 = C(g, 2 * t), c1 = C(g, 2 * t + 1);
+  dmma_8x8x4(c0, c1, A(g, t), B(t, g));
+  double e0 = C(g, 2 * t), e1 = C(g, 2 * t + 1);
+  for (int k = 0; k < 4; k++) {
+    e0 += A(g, k) * B(k, 2 * t);
+    e1 += A(g, k) * B(k, 2 * t + 1);
+  }
+  err[l] = fabs(c0 - e0) + fabs(c1 - e1);
+}
+
+// Throughput: MMA_CHAINS independent accumulators per warp; with dfma != 0
+// every DMMA is followed by PEAK_CHAINS independent DFMAs of the same warp,
+// so the two pipes' rates add up when they are separate units and share one
+// rate when they are one.  Every index stays inside the grid-sized buffer.
+constexpr int MMA_CHAINS = 4;
+__global__ void fp64_mma_peak_kernel(double* out, int iters, int dfma) {
+  const int l = threadIdx.x & 31;
+  const double a = 1.0 + 1e-3 * l, b = 1.0 - 1e-3 * l;
+  double c[MMA_CHAINS][2];
+#pragma unroll
+  for (int k = 0; k < MMA_CHAINS; k++) c[k][0] = c[k][1] = 1e-3 * k;
+  double f[PEAK_CHAINS];
+#pragma unroll
+  for (int k = 0; k < PEAK_CHAINS; k++) f[k] = 1.0 + k * 1e-3;
+  const double fb = 1.0000001 + 1e-9 * threadIdx.x, fc = 1e-7;
+  if (dfma) {
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+      for (int k = 0; k < MMA_CHAINS; k++) dmma_8x8x4(c[k][0], c[k][1], a, b);
+#pragma unroll
+      for (int k = 0; k < PEAK_CHAINS; k++) f[k] = fma(f[k], fb, fc);
+    }
+  } else {
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+      for (int k = 0; k < MMA_CHAINS; k++) dmma_8x8x4(c[k][0], c[k][1], a, b);
+    }
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < MMA_CHAINS; k++) s += c[k][0] + c[k][1];
+#pragma unroll
+  for (int k = 0; k < PEAK_CHAINS; k++) s += f[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 // ===================================================================== C ABI
 
 extern "C" {
@@ -1276,6 +1340,42 @@ int nbg_fp64_peak(nbg_context* ctx, double* tflops) {
     best = std::min(best, ms);
   }
   *tflops = 2.0 * (double)blocks * threads * iters * PEAK_CHAINS / (best * 1e-3) / 1e12;
+  return NBG_OK;
+}
+
+int nbg_fp64_mma_peak(nbg_context* ctx, int with_dfma, double* tflops, double* dfma_share) {
+  if (!ctx || !tflops) return set_error(NBG_EINVAL, "NULL argument");
+  NBG_CUDA(cudaSetDevice(ctx->device));
+  cudaDeviceProp p;
+  NBG_CUDA(cudaGetDeviceProperties(&p, ctx->device));
+  const int threads = 256, blocks = p.multiProcessorCount * 4, iters = 4000;
+  double* out;
+  int rc;
+  if ((rc = ctx->get("peak", (size_t)threads * blocks, &out))) return rc;
+  fp64_mma_check_kernel<<<1, 32, 0, ctx->stream>>>(out);
+  NBG_CUDA(cudaGetLastError());
+  double err[32];
+  NBG_CUDA(cudaMemcpyAsync(err, out, sizeof(err), cudaMemcpyDeviceToHost, ctx->stream));
+  NBG_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (int l = 0; l < 32; l++)
+    if (err[l] != 0.0) return set_error(NBG_EUNSUPPORTED, "DMMA fragment check: lane %d off by %g", l, err[l]);
+  fp64_mma_peak_kernel<<<blocks, threads, 0, ctx->stream>>>(out, 20, with_dfma);
+  NBG_CUDA(cudaGetLastError());
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; rep++) {
+    NBG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    fp64_mma_peak_kernel<<<blocks, threads, 0, ctx->stream>>>(out, iters, with_dfma);
+    NBG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    NBG_CUDA(cudaEventSynchronize(ctx->ev1));
+    float ms = 0;
+    NBG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    best = std::min(best, ms);
+  }
+  const double warps = (double)blocks * threads / 32.0;
+  const double mma_flops = warps * iters * MMA_CHAINS * 512.0;
+  const double fma_flops = with_dfma ? 2.0 * (double)blocks * threads * iters * PEAK_CHAINS : 0.0;
+  *tflops = (mma_flops + fma_flops) / (best * 1e-3) / 1e12;
+  if (dfma_share) *dfma_share = fma_flops / (mma_flops + fma_flops);
   return NBG_OK;
 }
 

@@ -104,6 +104,13 @@ extern "C" {
 
 int oracle_version(void) { return 1; }
 
+// Exact-zero entries of the operators skipped in the dense products (1) or
+// multiplied as the reference's mul! does (0, the default); both give
+// bitwise the same results for finite inputs.  Returns the previous setting.
+int oracle_set_skip_zero_products(int on) {
+  return skip_zero_products_flag().exchange(on != 0) ? 1 : 0;
+}
+
 // Transit Newton searches that stopped at ITMAX on this thread so far.
 long long oracle_newton_itmax_hits(void) { return newton_itmax_hits(); }
 
@@ -321,6 +328,52 @@ int oracle_fd_kepler_driftij(int n, int i, int j, double h, int drift_first, con
       }
   jac_num[6 + 14 * 6] = 1.0;
   jac_num[13 + 14 * 13] = 1.0;
+  return 0;
+}
+
+// Order-of-accuracy run of the no-gradient map, restating the energy study
+// of examples/energy_conservation.jl:96-183: nsteps of ahl21!(s, h) in
+// binary128 from (x, v), with the outer kick fraction 1/kick_den and
+// phisalpha!'s alpha (the method's values are 6 and 2; the pin passes others
+// to show that its test rejects them).  Returns the final x and v as
+// double-double pairs (hi = the rounded value, lo = the rest), so that end
+// states of different step sizes can be differenced far below double
+// precision, and the largest |E(t) - E(0)| / |E(0)| over the steps, E the
+// kinetic plus potential energy of compute_energy (:96-113).
+int oracle_order_run_quad(int n, double h, int64_t nsteps, const double* x, const double* v, const double* m,
+                          const uint8_t* pair, double kick_den, double alpha, double* x_hi, double* x_lo,
+                          double* v_hi, double* v_lo, double* max_rel_denergy) {
+  if (n < 2 || nsteps < 0) return -1;
+  State<quad> s;
+  load_state(s, n, x, v, m, nullptr, nullptr, nullptr, nullptr, nullptr, pair, nullptr);
+  const quad G = quad(GNEWT_D);
+  auto energy = [&]() {
+    quad ke = quad(0), pe = quad(0);
+    for (int j = 0; j < n; j++)
+      ke += quad(0.5) * s.m[j] * (s.V(0, j) * s.V(0, j) + s.V(1, j) * s.V(1, j) + s.V(2, j) * s.V(2, j));
+    for (int j = 0; j < n - 1; j++)
+      for (int k = j + 1; k < n; k++) {
+        quad dx = s.X(0, j) - s.X(0, k), dy = s.X(1, j) - s.X(1, k), dz = s.X(2, j) - s.X(2, k);
+        pe -= G * s.m[j] * s.m[k] / Mth<quad>::sqrt(dx * dx + dy * dy + dz * dz);
+      }
+    return ke + pe;
+  };
+  const quad e0 = energy();
+  quad worst = quad(0);
+  const quad hh = quad(h), kd = quad(kick_den), al = quad(alpha);
+  for (int64_t q = 0; q < nsteps; q++) {
+    ahl21_ng(s, hh, kd, al);
+    quad de = (energy() - e0) / e0;
+    if (de < quad(0)) de = -de;
+    if (de > worst) worst = de;
+  }
+  for (int q = 0; q < 3 * n; q++) {
+    x_hi[q] = (double)s.x[q];
+    x_lo[q] = (double)(s.x[q] - quad(x_hi[q]));
+    v_hi[q] = (double)s.v[q];
+    v_lo[q] = (double)(s.v[q] - quad(v_hi[q]));
+  }
+  *max_rel_denergy = (double)worst;
   return 0;
 }
 

@@ -28,6 +28,7 @@
 #include <cstring>
 #include <vector>
 #include <algorithm>
+#include <atomic>
 #if defined(__x86_64__) || defined(__i386__)
 #include <quadmath.h>
 #define NBGO_QUADMATH 1
@@ -207,9 +208,36 @@ template <class T> struct Derivs {
   T& DOT(int p, int di) { return dotdadq[p + 4 * di]; }
 };
 
+// Products skip the exact-zero entries of A when this flag is set (process
+// wide; off by default, so the CPU baseline multiplies every zero as the
+// reference's dense mul! does).  For finite B the skipped term is
+// fma(+-0, b, acc) = acc exactly, and acc is never -0 (it starts at +0 and
+// an FMA whose product is a signed zero and whose addend is +0 rounds to
+// +0), so both modes give bitwise the same C; tests/test_oracle_pins.py
+// checks that on whole integrations.  The long parity runs use it: the
+// operators of ahl21! are mostly structural zeros.
+inline std::atomic<bool>& skip_zero_products_flag() {
+  static std::atomic<bool> on(false);
+  return on;
+}
+inline bool skip_zero_products() { return skip_zero_products_flag().load(std::memory_order_relaxed); }
+
 // LinearAlgebra.mul!(C, A, B): C (m x p) = A (m x q) * B (q x p), col-major.
 template <class T>
 void mul(T* C, const T* A, const T* B, int m, int q, int p) {
+  if (skip_zero_products()) {
+    for (int j = 0; j < p; j++)
+      for (int i = 0; i < m; i++) {
+        T acc = T(0);
+        for (int k = 0; k < q; k++) {
+          const T a = A[i + (size_t)m * k];
+          if (a == T(0)) continue;
+          acc = Mth<T>::fma(a, B[k + (size_t)q * j], acc);
+        }
+        C[i + (size_t)m * j] = acc;
+      }
+    return;
+  }
   for (int j = 0; j < p; j++)
     for (int i = 0; i < m; i++) {
       T acc = T(0);

@@ -852,16 +852,19 @@ template <class T> void kepler_driftij_ng(State<T>& s, int i, int j, T h, bool d
     comp_sum(s.V(k, j), s.VE(k, j), (-mi) * s.delxv[3 + k]);
   }
 }
-// ahl21!(s, h) without Jacobian (ahl21_no_grad.jl:6-18)
-template <class T> void ahl21_ng(State<T>& s, T h) {
-  T h2 = T(0.5) * h, h6 = h / T(6);
+// ahl21!(s, h) without Jacobian (ahl21_no_grad.jl:6-18).  kick_den and alpha
+// are the method's constants (the outer kicks take h/6, phisalpha! alpha = 2);
+// only the order-of-accuracy pin passes other values, to show that the
+// convergence test detects a wrong coefficient.
+template <class T> void ahl21_ng(State<T>& s, T h, T kick_den = T(6), T alpha = T(2)) {
+  T h2 = T(0.5) * h, h6 = h / kick_den;
   kickfast_ng(s, h6);
   drift_ng(s, h2);
   for (int i = 0; i < s.n - 1; i++)  // drift_kepler! (:164-172)
     for (int j = i + 1; j < s.n; j++)
       if (!s.P(i, j)) kepler_driftij_ng(s, i, j, h2, true);
   phic_ng(s, h);
-  phisalpha_ng(s, h, T(2));
+  phisalpha_ng(s, h, alpha);
   for (int i = s.n - 2; i >= 0; i--)  // kepler_drift! (:178-186)
     for (int j = s.n - 1; j > i; j--)
       if (!s.P(i, j)) kepler_driftij_ng(s, i, j, h2, false);

@@ -44,7 +44,10 @@ def has_gpu():
         return False
 
 
-REF_ELEMENTS = "/root/reference/test/elements.txt"
+# The reference checkout whose test fixtures the CPU pins read in place;
+# NBG_REFERENCE_DIR overrides the default mount point.
+REF_DIR = os.environ.get("NBG_REFERENCE_DIR", "/root/reference")
+REF_ELEMENTS = os.path.join(REF_DIR, "test", "elements.txt")
 
 
 @pytest.fixture(scope="session")

@@ -1,0 +1,162 @@
+"""Parity at the benchmark configurations' full integration spans.
+
+Each test integrates a whole benchmark batch on the GPU, over every system's
+own full span, and compares a sample of its systems with the oracle run over
+the same span on host threads (concurrently with the GPU run):
+
+  * batch_3body  (4096 x 3 bodies, h = 0.5 d, 1000 d): 32 systems;
+  * batch_8body  (1024 x 8 bodies, h = 0.06 d, 1600 d = 26 667 steps):
+    8 systems, the first and the last among them;
+  * batch_uneven (2048 systems, N = 2..10, up to 77 k steps): the longest
+    system of each body count from 8 to 10 and of the 9- and 10-body systems
+    over 3000 d, and the shortest system of every body count.
+
+The tolerances are those of tests/parity.py (tt 1e-10 of the span, dtdq0 and
+dtdelements 1e-8 relative).  Each test also writes its worst tolerance ratios
+(error / tolerance, 1.0 = at the bound) to the JSON-lines file named by
+NBG_PARITY_REPORT when that variable is set.
+
+The oracle multiplies its operators with the exact-zero entries skipped:
+bitwise the same results as its dense products (tests/test_oracle_pins.py),
+several times faster at 8-10 bodies.
+"""
+import json
+import os
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+import pytest
+
+import nbg
+import oracle_lib as O
+import parity as P
+from conftest import has_gpu
+from nbg import workloads as W
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not has_gpu(), reason="needs a CUDA GPU")]
+
+
+def _report(name, **vals):
+    path = os.environ.get("NBG_PARITY_REPORT")
+    if path:
+        with open(path, "a") as f:
+            f.write(json.dumps(dict(test=name, **vals)) + "\n")
+
+
+def _oracle_runs(jobs):
+    """Runs (state, h, tmax, ntt) jobs through the oracle on host threads; returns a future of
+    [(OState, OTiming)].  ctypes releases the GIL, so the GPU run proceeds meanwhile."""
+    threads = max(1, (os.cpu_count() or 2) - 2)
+
+    def one(job):
+        s, h, tmax, ntt = job
+        so = O.OState(s.x, s.v, s.m, jac_init=s.jac_init)
+        to = O.OTiming(s.n, ntt, 0)
+        O.integrate_transits(so, to, h, tmax)
+        return so, to
+
+    ex = ThreadPoolExecutor(max_workers=min(threads, len(jobs)))
+    cm = O.skip_zero_products()
+    cm.__enter__()
+    futs = [ex.submit(one, j) for j in jobs]
+
+    class Runs:
+        def result(self):
+            try:
+                return [f.result() for f in futs]
+            finally:
+                ex.shutdown()
+                cm.__exit__(None, None, None)
+
+    return Runs()
+
+
+def _gpu_batch(states, hs, tms, ntts):
+    b = nbg.Batch([s.n for s in states], 0, hs, tms, ntts, True)
+    for q, s in enumerate(states):
+        b.set_system(q, s)
+    return b
+
+
+def _compare_system(b, q, so, to, tmax):
+    """Worst tolerance ratios of system q of the GPU batch against the oracle run."""
+    n = int(b.n[q])
+    ntt = int(b.ntt[q])
+    M = 7 * n
+    P.check_counts(b.view("count", q), to.count)
+    err_tt = P.check_tt(b.view("tt", q).reshape((n, ntt), order="F"), to.tt, to.count, tmax)
+    r_dq = P.check_transit_derivs(b.view("dtdq0", q).reshape((n, ntt, 7, n), order="F"), to.dtdq0, to.count)
+    r_de = P.check_transit_derivs(b.view("dtdelements", q).reshape((n, ntt, 7, n), order="F"), to.dtdelements,
+                                  to.count, "dtdelements", to.dtdq0, so.jac_init)
+    gs = type("S", (), {})()
+    gs.x = b.view("x", q).reshape((3, n), order="F")
+    gs.v = b.view("v", q).reshape((3, n), order="F")
+    gs.jac_step = b.view("jac_step", q).reshape((M, M), order="F")
+    gs.dqdt = b.view("dqdt", q)
+    P.check_state(gs, so)
+    return {"n": n, "transits": int(to.count.sum()), "tt": err_tt / (P.TT_TOL * abs(tmax)), "dtdq0": r_dq,
+            "dtdelements": r_de}
+
+
+def _run_and_compare(name, states, hs, tms, ntts, sample):
+    jobs = [(states[q], hs[q], tms[q], ntts[q]) for q in sample]
+    runs = _oracle_runs(jobs)
+    b = _gpu_batch(states, hs, tms, ntts)
+    b.run()
+    bad = nbg._lib.NBG_STATUS_NONFINITE | nbg._lib.NBG_STATUS_NTT_OVERFLOW
+    assert np.all((b.status & bad) == 0)
+    results = runs.result()
+    rows = []
+    for q, (so, to) in zip(sample, results):
+        r = _compare_system(b, q, so, to, tms[q])
+        r.update(system=int(q), steps=int(abs(round(tms[q] / hs[q]))))
+        rows.append(r)
+    worst = {k: max(r[k] for r in rows) for k in ("tt", "dtdq0", "dtdelements")}
+    _report(name, systems=len(states), sample=len(sample), worst=worst, rows=rows)
+    return worst
+
+
+def test_c1_full_batch_sample_of_32():
+    """batch_3body: 4096 systems x 2000 steps; 32 systems spread over the batch against the oracle."""
+    els, h, tmax = W.batch_3body(4096, seed=0)
+    states = [nbg.State(W.ic_of(el)) for el in els]
+    ntt = nbg.TransitTiming(tmax, W.ic_of(els[0])).ntt
+    sample = sorted(set(np.linspace(0, len(els) - 1, 32).astype(int).tolist()))
+    worst = _run_and_compare("batch_3body", states, [h] * len(els), [tmax] * len(els), [ntt] * len(els), sample)
+    assert max(worst.values()) <= 1.0
+
+
+def test_c2_full_span():
+    """batch_8body: 1024 systems x 26 667 steps (1600 d); 8 systems, q = 0 and 1023 among them."""
+    els, h, tmax = W.batch_8body(1024, seed=0)
+    states = [nbg.State(W.ic_of(el)) for el in els]
+    # every system's periods are within a few 1e-3 of each other: one transit array shape, with margin
+    ntt = max(nbg.TransitTiming(tmax, W.ic_of(el)).ntt for el in els) + 2
+    sample = [0, 1, 146, 292, 511, 731, 877, 1023]
+    worst = _run_and_compare("batch_8body", states, [h] * len(els), [tmax] * len(els), [ntt] * len(els), sample)
+    assert max(worst.values()) <= 1.0
+
+
+def test_c3_full_span_longest_and_shortest():
+    """batch_uneven: 2048 systems, N = 2..10, every system over its own span (up to 77 k steps): the
+    longest system of N = 8, 9 and 10, the longest 9- and 10-body systems beyond 3000 d, and the
+    shortest system of every body count against the oracle."""
+    els, hs, tms = W.batch_uneven(2048, seed=0)
+    ics = [W.ic_of(el) for el in els]
+    states = [nbg.State(ic) for ic in ics]
+    ntts = [nbg.TransitTiming(tm, ic).ntt for tm, ic in zip(tms, ics)]
+    ns = np.array([s.n for s in states])
+    steps = np.array([abs(round(t / h)) for t, h in zip(tms, hs)])
+    sample = set()
+    for n in (8, 9, 10):
+        idx = np.where(ns == n)[0]
+        sample.add(int(idx[np.argmax(steps[idx])]))
+    for n in (9, 10):
+        idx = np.where((ns == n) & (np.array(tms) > 3000.0))[0]
+        sample.add(int(idx[np.argmax(steps[idx])]))
+    for n in range(2, 11):
+        idx = np.where(ns == n)[0]
+        sample.add(int(idx[np.argmin(steps[idx])]))
+    sample = sorted(sample, key=lambda q: -steps[q])  # longest oracle runs first
+    worst = _run_and_compare("batch_uneven", states, hs, tms, ntts, sample)
+    assert max(worst.values()) <= 1.0

@@ -14,6 +14,8 @@ import tempfile
 
 import pytest
 
+import nbg
+
 from conftest import PKG_DIR, has_gpu
 
 pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not has_gpu(), reason="needs a CUDA GPU")]
@@ -97,3 +99,16 @@ def test_kepler_math_against_cuda_and_series():
     assert sin_ulp <= 2.0, sin_ulp
     assert cos_ulp <= 2.0, cos_ulp
     assert series_rel <= 1e-15, series_rel  # a few ulp: polynomial vs term-by-term rounding
+
+
+def test_fp64_tensor_core_probe_runs_and_checks_its_fragments():
+    """The DMMA probe checks one exact m8n8k4 f64 product against the documented fragment layout (it
+    fails with NBG_EUNSUPPORTED otherwise) and reports positive rates."""
+    ctx = nbg.Context(0)
+    try:
+        mma, share0 = ctx.fp64_mma_peak_tflops(False)
+        mixed, share = ctx.fp64_mma_peak_tflops(True)
+    finally:
+        ctx.close()
+    assert mma > 0 and mixed > 0
+    assert share0 == 0.0 and 0.0 < share < 1.0

@@ -342,3 +342,35 @@ def test_init_nbody_jacobian_double_binary():
         mapped[:, 7 * (i + 1):7 * (i + 1) + 6] = num[:, 7 * r:7 * r + 6]
     assert close(jac, mapped)
     assert not close(jac, num)  # the row-by-row layout differs for this hierarchy
+
+
+@pytest.mark.parametrize("kick", [False, True])
+def test_skip_zero_products_is_bitwise_dense(kick):
+    """The oracle's zero-skipping products (used by the long GPU parity runs) give bitwise the dense
+    products' integration: state, Jacobian, transit times and their derivatives."""
+    el, h, _ = W.plain_3body(3)
+    if kick:
+        el = np.vstack([el, [2e-5, 41.0, 7.0, 0.01, -0.02, np.pi / 2, 0.0]])
+    n = el.shape[0]
+    x, v, jinit = O.init_nbody(el, 0.0)
+    pair = np.zeros((n, n), dtype=np.uint8)
+    if kick:
+        pair[0, 3] = pair[3, 0] = 1
+    tmax = 60.0
+    out = []
+    for skip in (False, True):
+        s = O.OState(x, v, el[:, 0], jac_init=jinit, pair=pair)
+        t = O.OTiming(n, O.ntt_for(tmax, el[1:, 1]), 0)
+        if skip:
+            with O.skip_zero_products():
+                O.integrate_transits(s, t, h, tmax)
+        else:
+            O.integrate_transits(s, t, h, tmax)
+        out.append((s, t))
+    (a, ta), (b, tb) = out
+    assert int(ta.count.sum()) > 0
+    for k in ("x", "v", "xerror", "verror", "jac_step", "jac_error", "dqdt"):
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
+    for k in ("tt", "dtdq0", "dtdelements", "count"):
+        assert np.array_equal(getattr(ta, k), getattr(tb, k)), k
+    assert O.lib().oracle_set_skip_zero_products(0) == 0  # the context manager restored the default
