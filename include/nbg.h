@@ -280,9 +280,23 @@ int nbg_batch_integrate_transits_device(nbg_context* ctx, int nsys, const nbg_sy
  * and a message naming the sizes; larger batches fit by shortening the
  * chunk, at some speed.
  *
- * The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture on the device.  Every call on a device shares
+ * Every call looks up the array's device address (cudaGetSymbolAddress) with
+ * the context's device current.  Under CUDA's lazy module loading (the
+ * default) the first call on a device loads the library's module there and
+ * reserves the 64 MiB array at that moment: a caller that reserves the rest
+ * of the GPU's memory for itself must make one call (any small batch) before
+ * doing so, or that first lookup fails with NBG_ECUDA (out of memory); make
+ * that first call before any stream capture on the device, too.  With
+ * CUDA_MODULE_LOADING=EAGER every context reserves the array when it is
+ * created, whether it calls this entry point or not.  The host bookkeeping
+ * (about 90 KB) belongs to the context and is allocated by nbg_create.
+ *
+ * Speed: the call runs every kernel on the context's one stream, without the
+ * producer / consumer overlap of the other batched entry points, and its
+ * chunk shrinks when the working set would not fit; expect it to be slower
+ * than nbg_batch_integrate_transits_device on the same batch.
+ *
+ * Every call on a device shares
  * the one array and finds the previous call's contents in it (the call
  * clears what must start at zero itself).  Calls that overlap on the GPU --
  * from two threads, two contexts or two streams of the same device -- race
@@ -316,7 +330,8 @@ int nbg_batch_integrate_transits_noalloc(nbg_context* ctx, int nsys, const nbg_s
  * slot buffers (a request whose new group does not fit fails NBG_ENOMEM).
  * Results are bitwise the same whether a request runs alone or among others.
  * Requests not yet admitted when the server stops are cancelled
- * (NBG_ECANCELLED); admitted ones run to completion.
+ * (NBG_ECANCELLED); admitted ones run to completion.  nbg_server_cancel
+ * withdraws one request at any time before its last chunk is queued.
  */
 typedef struct nbg_server nbg_server;
 
@@ -377,7 +392,20 @@ int nbg_server_poll(nbg_server* srv, int64_t id, int32_t timeout_ms, double* t, 
 
 int nbg_server_stats(nbg_server* srv, nbg_server_stats_t* out);
 
-/* Cancel requests not yet admitted, finish the running ones, free the server. */
+/* Withdraw request `id` (no reference counterpart: the reference has no
+ * request queue).  A request not yet admitted leaves its queue; a running one
+ * is retired at the next chunk boundary of its group, its slot and output
+ * memory freed; nbg_server_poll of either returns NBG_ECANCELLED.  Returns
+ * NBG_OK when the cancellation took effect, NBG_EINVAL for an unknown or
+ * already collected id, or for a request that has finished or whose last
+ * chunk is already queued (its result stands and is collected as usual). */
+int nbg_server_cancel(nbg_server* srv, int64_t id);
+
+/* Cancel requests not yet admitted (their nbg_server_poll returns
+ * NBG_ECANCELLED), finish the running ones, wait for threads still inside
+ * nbg_server_wait_any / nbg_server_poll to return (a wait_any with nothing
+ * left to collect returns NBG_ECANCELLED), then free the server.  Requests
+ * not collected by then are freed with it. */
 int nbg_server_stop(nbg_server* srv);
 
 /* Tuning knobs of a context (no reference counterpart).  Results do not

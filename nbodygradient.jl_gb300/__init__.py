@@ -28,13 +28,13 @@ import numpy as np
 os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 from . import _lib, build, workloads
-from ._lib import Context, NbgError, SystemDesc, default_context, device_info
+from ._lib import Context, NbgError, NonFiniteWarning, SystemDesc, default_context, device_info
 from .ics import CartesianIC, Elements, ElementsIC, hierarchy, hierarchy_nested, init_nbody, kepler_init
 
 __all__ = ["Elements", "ElementsIC", "CartesianIC", "State", "TransitTiming", "TransitParameters", "CartesianOutput",
            "Integrator",
            "ahl21", "set_state", "initialize", "dState", "Derivatives",
-           "Context", "NbgError", "default_context", "device_info", "integrate_transits_batch", "Batch", "Server",
+           "Context", "NbgError", "NonFiniteWarning", "default_context", "device_info", "integrate_transits_batch", "Batch", "Server",
            "init_nbody_batch", "hierarchy",
            "hierarchy_nested", "init_nbody", "kepler_init"]
 
@@ -233,8 +233,10 @@ class Integrator:
         intr(s; grad)                       Integrator.jl:247 (to s.t + tmax)
         intr(s, o::CartesianOutput)         Outputs.jl:26
 
-        grad is keyword-only, as in the reference.  return_arrays=True returns None: the step scratch the
-        reference would hand back lives on the device."""
+        grad is keyword-only, as in the reference.  return_arrays=True returns a Derivatives for the
+        three-argument form, as the reference does (a fresh one: the step scratch itself lives on the device).
+        A State that ends non-finite raises NonFiniteWarning (the reference propagates the values silently);
+        the outputs are written as computed."""
         if d is not None:
             if not isinstance(d, Derivatives):
                 raise TypeError("the third argument of intr(s, tt, d) is a Derivatives (dState(ic) makes one)")
@@ -251,11 +253,11 @@ class Integrator:
             if tt is None:
                 tt = float(s.t[0] + self.tmax)
             if isinstance(tt, (int, np.integer)) and not isinstance(tt, bool):
-                _lib.check(L.nbg_integrate_steps(ctx.handle, s.n, self.h, int(tt), int(bool(grad)), *args))
+                _lib.check_values(L.nbg_integrate_steps(ctx.handle, s.n, self.h, int(tt), int(bool(grad)), *args))
                 if self.h < 0:  # intr(s, N) leaves intr.h positive (Integrator.jl:228-229)
                     self.h = -self.h
             else:
-                _lib.check(L.nbg_integrate(ctx.handle, s.n, self.h, float(tt), int(bool(grad)), *args))
+                _lib.check_values(L.nbg_integrate(ctx.handle, s.n, self.h, float(tt), int(bool(grad)), *args))
             return None
         if isinstance(tt, CartesianOutput):
             if tt.nbody != s.n:
@@ -264,7 +266,7 @@ class Integrator:
             xr = np.zeros((tt.nstep, 3 * s.n))
             vr = np.zeros((tt.nstep, 3 * s.n))
             jr = None if tt.jac_step is None else np.zeros((tt.nstep, 49 * s.n * s.n))
-            _lib.check(L.nbg_integrate_cartesian(
+            _lib.check_values(L.nbg_integrate_cartesian(
                 ctx.handle, s.n, self.h, self.tmax, tt.nstep, p(s.t), p(s.x), p(s.v), p(s.m), p(s.xerror),
                 p(s.verror), p(s.jac_step), p(s.jac_error), p(s.dqdt), p(s.pair, _lib._U8), p(tt.t), p(xr), p(vr),
                 p(jr)))
@@ -275,18 +277,22 @@ class Integrator:
                     tt.jac_step[i] = jr[i].reshape((7 * s.n, 7 * s.n), order="F")
             return None
         if isinstance(tt, TransitParameters):
-            _lib.check(L.nbg_integrate_transit_parameters(
+            _lib.check_values(L.nbg_integrate_transit_parameters(
                 ctx.handle, s.n, tt.ti - 1, self.h, self.tmax, int(bool(grad)), p(s.t), p(s.x), p(s.v), p(s.m),
                 p(s.xerror), p(s.verror), p(s.jac_step), p(s.jac_error), p(s.dqdt), p(s.pair, _lib._U8),
                 p(s.jac_init), tt.ntt, p(tt.ttbv), p(tt.dtbvdq0), p(tt.dtbvdelements), p(tt.count, _lib._I64)))
-            return None
+            return Derivatives(s.n) if return_arrays and d is None else None
         if not isinstance(tt, TransitTiming):
             raise NbgError(_lib.NBG_EUNSUPPORTED,
                            "intr(s, tt) takes a TransitTiming, a TransitParameters, a time or a step count")
-        _lib.check(L.nbg_integrate_transits(
+        _lib.check_values(L.nbg_integrate_transits(
             ctx.handle, s.n, tt.ti - 1, self.h, self.tmax, int(bool(grad)), p(s.t), p(s.x), p(s.v), p(s.m),
             p(s.xerror), p(s.verror), p(s.jac_step), p(s.jac_error), p(s.dqdt), p(s.pair, _lib._U8), p(s.jac_init),
             tt.ntt, p(tt.tt), p(tt.dtdq0), p(tt.dtdelements), p(tt.count, _lib._I64)))
+        # intr(s, tt; return_arrays=true) hands back the step scratch for later three-argument calls
+        # (Transits.jl:173-180); the scratch of this path lives on the device, so a fresh Derivatives is
+        # returned (usable the same way; its contents are not the last step's scratch)
+        return Derivatives(s.n) if return_arrays and d is None else None
 
 
 class Batch:
@@ -539,6 +545,11 @@ class Server:
             p(s.jac_error), p(s.dqdt), p(tt.tt), p(tt.dtdq0), p(tt.dtdelements), p(tt.count, _lib._I64),
             ctypes.byref(info)))
         return {k: getattr(info, k) for k, _ in _lib.RequestInfo._fields_}
+
+    def cancel(self, rid):
+        """Withdraw request rid (nbg_server_cancel): result(rid, ...) then raises NbgError with
+        NBG_ECANCELLED.  Raises NbgError (NBG_EINVAL) when the request has already finished."""
+        _lib.check(_lib.load().nbg_server_cancel(self._h, int(rid)))
 
     def stats(self):
         import ctypes

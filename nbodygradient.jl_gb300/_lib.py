@@ -38,7 +38,7 @@ EXPORTS = (
     "nbg_integrate_transit_parameters", "nbg_batch_integrate_transit_parameters",
     "nbg_batch_init_nbody", "nbg_batch_init_nbody_device", "nbg_integrate_cartesian", "nbg_autotune_device",
     "nbg_server_start", "nbg_server_enqueue", "nbg_server_wait_any", "nbg_server_poll", "nbg_server_stats",
-    "nbg_server_stop", "nbg_batch_create", "nbg_batch_submit", "nbg_batch_run", "nbg_batch_wait",
+    "nbg_server_cancel", "nbg_server_stop", "nbg_batch_create", "nbg_batch_submit", "nbg_batch_run", "nbg_batch_wait",
     "nbg_batch_destroy",
 )
 
@@ -156,6 +156,7 @@ def load(build_if_missing=True):
                                   _I64, ctypes.POINTER(RequestInfo)]
     L.nbg_server_stats.argtypes = [_VP, ctypes.POINTER(ServerStats)]
     L.nbg_server_stop.argtypes = [_VP]
+    L.nbg_server_cancel.argtypes = [_VP, ctypes.c_int64]
     L.nbg_batch_create.argtypes = [_VP, ctypes.c_int, ctypes.POINTER(SystemDesc), ctypes.POINTER(_VP)]
     L.nbg_batch_submit.argtypes = [_VP, _D, _D, _D, _D, _D, _D, _D, _D, _D, _U8, _D, _D, _D, _D, _I64, _U32]
     L.nbg_batch_run.argtypes = [_VP]
@@ -175,6 +176,20 @@ def check(rc):
     if rc != NBG_OK:
         raise NbgError(rc, last_error())
     return rc
+
+
+class NonFiniteWarning(RuntimeWarning):
+    """A system's x, v or jac_step ended non-finite (NBG_ENONFINITE)."""
+
+
+def check_values(rc):
+    """check() for the reference-facing calls: NBG_ENONFINITE becomes a warning, because the reference
+    lets non-finite values propagate into the State without raising (the outputs are written as computed)."""
+    if rc == NBG_ENONFINITE:
+        import warnings
+        warnings.warn(last_error(), NonFiniteWarning, stacklevel=3)
+        return rc
+    return check(rc)
 
 
 def ptr(a, ctype=_D):

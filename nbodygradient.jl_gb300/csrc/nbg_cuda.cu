@@ -231,6 +231,29 @@ struct Buf {
   size_t bytes = 0;
 };
 
+constexpr int kNaMax = NBG_NOALLOC_MAX_SYSTEMS;
+
+// Host bookkeeping of nbg_batch_integrate_transits_noalloc (about 90 KB): one
+// per context, allocated with the context, so that the call itself allocates
+// nothing and needs little of its caller's stack.
+struct NoallocPlan {
+  SysOff off[kNaMax];
+  long long offtt[kNaMax], offdq[kNaMax], nsteps[kNaMax];
+  double hsig[kNaMax], t0[kNaMax], tout[kNaMax];
+  uint8_t pair[kNaMax * NBG_MAX_BODIES * NBG_MAX_BODIES];
+  int order[kNaMax];                 // systems by group, longest first within a group
+  int ngroups, gstart[kNaMax + 1];   // group q owns order[gstart[q] .. gstart[q+1])
+  int gN[kNaMax], ggrad[kNaMax], gof[kNaMax];
+  unsigned long long gkick[kNaMax];
+  long long gmax[kNaMax];
+  GroupArgs g[kNaMax];
+  // per-group staging of the scalars copied to the device, and the status read back
+  int sidx[kNaMax], vntt[kNaMax], vti[kNaMax];
+  double vt0[kNaMax], vh[kNaMax], vhI[kNaMax];
+  long long vns[kNaMax];
+  unsigned sv[kNaMax];
+};
+
 }  // namespace
 
 struct nbg_context {
@@ -253,6 +276,7 @@ struct nbg_context {
   // stream and a transit-search stream (gstreams[3q .. 3q+2])
   std::vector<cudaStream_t> gstreams;
   std::vector<cudaEvent_t> sync_events;  // cross-stream ordering, no timing
+  NoallocPlan* noalloc = nullptr;         // host plan of the allocation-free entry point
 
   int sync_event(size_t i, cudaEvent_t* out) {
     while (sync_events.size() <= i) {
@@ -802,7 +826,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
 // nbg_batch_integrate_transits_noalloc runs the same kernels in the same
 // order as run_batch, but takes every device buffer from the fixed scratch
 // array of nbg_noalloc.cu (bump allocation, 256-byte aligned) and keeps its
-// host bookkeeping on the stack.  The steps per chunk (and the transit
+// host bookkeeping in the context's NoallocPlan.  The steps per chunk (and the transit
 // kernel's thread count) shrink until the working set fits; neither changes
 // the arithmetic of any system.
 
@@ -820,21 +844,6 @@ struct ScratchArena {
     used = at + bytes;
     *out = base ? (T*)(base + at) : nullptr;
   }
-};
-
-constexpr int kNaMax = NBG_NOALLOC_MAX_SYSTEMS;
-
-struct NoallocPlan {
-  SysOff off[kNaMax];
-  long long offtt[kNaMax], offdq[kNaMax], nsteps[kNaMax];
-  double hsig[kNaMax], t0[kNaMax], tout[kNaMax];
-  uint8_t pair[kNaMax * NBG_MAX_BODIES * NBG_MAX_BODIES];
-  int order[kNaMax];                 // systems by group, longest first within a group
-  int ngroups, gstart[kNaMax + 1];   // group q owns order[gstart[q] .. gstart[q+1])
-  int gN[kNaMax], ggrad[kNaMax];
-  unsigned long long gkick[kNaMax];
-  long long gmax[kNaMax];
-  GroupArgs g[kNaMax];
 };
 
 // Carves the device buffers of every group for chunk length K and transit
@@ -900,7 +909,7 @@ int run_batch_noalloc(nbg_context* ctx, NoallocPlan& P, int nsys, const nbg_syst
   NBG_CUDA(cudaMemcpyAsync(P.pair, d_pair, (size_t)ap, cudaMemcpyDeviceToHost, st));
   NBG_CUDA(cudaStreamSynchronize(st));
   P.ngroups = 0;
-  int gof[kNaMax];
+  int* gof = P.gof;
   for (int s = 0; s < nsys; s++) {
     const int n = desc[s].n;
     P.nsteps[s] = steps_of(desc[s].h, desc[s].tmax);
@@ -992,9 +1001,9 @@ int run_batch_noalloc(nbg_context* ctx, NoallocPlan& P, int nsys, const nbg_syst
     GroupArgs& g = P.g[q];
     const int N = g.N, S = g.S;
     g.tt = d_tt; g.off_tt = d_offtt; g.dtdq0 = d_dq0; g.off_dq = d_offdq;
-    int sidx[kNaMax], vntt[kNaMax], vti[kNaMax];
-    double vt0[kNaMax], vh[kNaMax], vhI[kNaMax];
-    long long vns[kNaMax];
+    int *sidx = P.sidx, *vntt = P.vntt, *vti = P.vti;
+    double *vt0 = P.vt0, *vh = P.vh, *vhI = P.vhI;
+    long long* vns = P.vns;
     for (int r = 0; r < S; r++) {
       sidx[r] = -1; vntt[r] = 1; vti[r] = 0; vt0[r] = vh[r] = vhI[r] = 0.0; vns[r] = 0;
     }
@@ -1011,7 +1020,7 @@ int run_batch_noalloc(nbg_context* ctx, NoallocPlan& P, int nsys, const nbg_syst
     NBG_CUDA(cudaMemcpyAsync(g.hI, vhI, sizeof(double) * S, cudaMemcpyHostToDevice, st));
     NBG_CUDA(cudaMemcpyAsync(g.nsteps, vns, sizeof(long long) * S, cudaMemcpyHostToDevice, st));
     NBG_CUDA(cudaMemsetAsync(g.status, 0, sizeof(unsigned) * S, st));
-    NBG_CUDA(cudaStreamSynchronize(st));  // the staging arrays go out of scope
+    NBG_CUDA(cudaStreamSynchronize(st));  // the next group reuses the staging arrays
     const int pb = (S + 127) / 128;
     pack_state_kernel<<<pb, 128, 0, st>>>(N, S, g.sysidx, d_off, d_x, d_v, d_xe, d_ve, d_m, d_dqdt, d_count, g.x,
                                           g.v, g.xe, g.ve, g.m, g.dqdt, g.count);
@@ -1092,7 +1101,7 @@ int run_batch_noalloc(nbg_context* ctx, NoallocPlan& P, int nsys, const nbg_syst
     std::fill(status_host, status_host + nsys, 0u);
     for (int q = 0; q < P.ngroups; q++) {
       const GroupArgs& g = P.g[q];
-      unsigned sv[kNaMax];
+      unsigned* sv = P.sv;
       NBG_CUDA(cudaMemcpy(sv, g.status, sizeof(unsigned) * g.S, cudaMemcpyDeviceToHost));
       for (int r = 0; r < g.nsys; r++) status_host[P.order[P.gstart[q] + r]] = sv[r];
     }
@@ -1221,6 +1230,7 @@ int nbg_create(int device, nbg_context** out) {
   NBG_CUDA(cudaSetDevice(device));
   nbg_context* c = new nbg_context();
   c->device = device;
+  c->noalloc = new NoallocPlan();
   {
     cudaDeviceProp p;
     if (cudaGetDeviceProperties(&p, device) == cudaSuccess) c->sm_count = p.multiProcessorCount;
@@ -1248,6 +1258,7 @@ int nbg_destroy(nbg_context* ctx) {
   for (auto e : ctx->sync_events) cudaEventDestroy(e);
   for (cudaStream_t s2 : ctx->gstreams) cudaStreamDestroy(s2);
   cudaStreamDestroy(ctx->stream);
+  delete ctx->noalloc;
   delete ctx;
   return NBG_OK;
 }
@@ -1451,6 +1462,17 @@ static int batch_host_device(nbg_context* ctx, int nsys, const nbg_system_desc* 
 
 // Plain integration of nsys systems (host arrays, the packed layout of the
 // batched calls; no transit arrays).
+// NBG_ENONFINITE (after every output has been written) when a system ended
+// with a non-finite x, v or jac_step: the entry points without a status array
+// report it this way; the reference lets the values propagate silently.
+static int nonfinite_error(int nsys, const uint32_t* status) {
+  for (int s = 0; s < nsys; s++)
+    if (status[s] & NBG_STATUS_NONFINITE)
+      return set_error(NBG_ENONFINITE, "system %d: x, v or jac_step is not finite at the end of the integration "
+                                       "(outputs written as computed)", s);
+  return NBG_OK;
+}
+
 static int plain_host(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const PlainSpec* spec, double* t,
                       double* x, double* v, const double* m, double* xerror, double* verror, double* jac_step,
                       double* jac_error, double* dqdt, const uint8_t* pair, const TrajOut* traj = nullptr) {
@@ -1484,8 +1506,9 @@ static int plain_host(nbg_context* ctx, int nsys, const nbg_system_desc* desc, c
   NBG_CUDA(cudaMemcpyAsync(d_E, jac_error, sizeof(double) * aJ, cudaMemcpyHostToDevice, st));
   NBG_CUDA(cudaMemcpyAsync(d_dq, dqdt, sizeof(double) * adq, cudaMemcpyHostToDevice, st));
   NBG_CUDA(cudaMemsetAsync(d_cnt, 0, sizeof(long long) * am, st));
+  std::vector<uint32_t> stv(nsys, 0u);
   rc = run_batch(ctx, nsys, desc, t, pair, d_t, d_x, d_v, d_m, d_xe, d_ve, d_J, d_E, d_dq, nullptr, nullptr, nullptr,
-                 nullptr, d_cnt, nullptr, spec, 0, traj);
+                 nullptr, d_cnt, stv.data(), spec, 0, traj);
   if (rc) return rc;
   NBG_CUDA(cudaMemcpyAsync(t, d_t, sizeof(double) * nsys, cudaMemcpyDeviceToHost, st));
   NBG_CUDA(cudaMemcpyAsync(x, d_x, sizeof(double) * ax, cudaMemcpyDeviceToHost, st));
@@ -1496,7 +1519,7 @@ static int plain_host(nbg_context* ctx, int nsys, const nbg_system_desc* desc, c
   NBG_CUDA(cudaMemcpyAsync(jac_error, d_E, sizeof(double) * aJ, cudaMemcpyDeviceToHost, st));
   NBG_CUDA(cudaMemcpyAsync(dqdt, d_dq, sizeof(double) * adq, cudaMemcpyDeviceToHost, st));
   NBG_CUDA(cudaStreamSynchronize(st));
-  return NBG_OK;
+  return nonfinite_error(nsys, stv.data());
 }
 
 // intr(s, time) (Integrator.jl:159-197): nsteps = |round((time - t0)/h)|
@@ -1610,8 +1633,10 @@ int nbg_integrate_transits(nbg_context* ctx, int n, int ti, double h, double tma
   if (n < NBG_MIN_BODIES || n > NBG_MAX_BODIES)
     return set_error(NBG_EUNSUPPORTED, "n = %d outside %d..%d", n, NBG_MIN_BODIES, NBG_MAX_BODIES);
   if (ti < 0 || ti >= n) return set_error(NBG_EINVAL, "ti = %d not in 0..%d", ti, n - 1);
-  return batch_host_device(ctx, 1, &d, t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair, jac_init, tt,
-                           dtdq0, dtdelements, count, nullptr, true);
+  uint32_t st1 = 0;
+  const int rc = batch_host_device(ctx, 1, &d, t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair, jac_init,
+                                   tt, dtdq0, dtdelements, count, &st1, true);
+  return rc ? rc : nonfinite_error(1, &st1);
 }
 
 static void* ctx_scratch(void* c, const char* name, size_t bytes) {
@@ -1670,8 +1695,10 @@ int nbg_integrate_transit_parameters(nbg_context* ctx, int n, int ti, double h, 
   if (ti < 0 || ti >= n) return set_error(NBG_EINVAL, "ti = %d not in 0..%d", ti, n - 1);
   nbg_system_desc d;
   d.n = n; d.ti = ti; d.grad = grad ? 1 : 0; d.ntt = (int32_t)ntt; d.h = h; d.tmax = tmax;
-  return batch_host_device(ctx, 1, &d, t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair, jac_init, ttbv,
-                           dtbvdq0, dtbvdelements, count, nullptr, true, 1);
+  uint32_t st1 = 0;
+  const int rc = batch_host_device(ctx, 1, &d, t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair, jac_init,
+                                   ttbv, dtbvdq0, dtbvdelements, count, &st1, true, 1);
+  return rc ? rc : nonfinite_error(1, &st1);
 }
 
 int nbg_batch_integrate_transit_parameters(nbg_context* ctx, int nsys, const nbg_system_desc* desc, double* t,
@@ -1861,8 +1888,7 @@ int nbg_batch_integrate_transits_noalloc(nbg_context* ctx, int nsys, const nbg_s
     return set_error(NBG_EINVAL, "nbg_batch_integrate_transits_noalloc: nsys = %d not in 1..%d (NBG_NOALLOC_MAX_SYSTEMS)",
                      nsys, NBG_NOALLOC_MAX_SYSTEMS);
   NBG_CUDA(cudaSetDevice(ctx->device));
-  NoallocPlan plan;
-  return run_batch_noalloc(ctx, plan, nsys, desc, t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair,
+  return run_batch_noalloc(ctx, *ctx->noalloc, nsys, desc, t, x, v, m, xerror, verror, jac_step, jac_error, dqdt, pair,
                            jac_init, tt, dtdq0, dtdelements, (long long*)count, status);
 }
 

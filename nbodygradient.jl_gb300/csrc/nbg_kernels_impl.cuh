@@ -50,7 +50,10 @@ __global__ void __launch_bounds__(PROD_BS * PROD_MAX_WARPS) orbit_chunk_kernel(G
   const double t0 = g.t0[s], h = g.h[s], hI = g.hI[s];
   const int ntt = g.ntt[s], ti = g.ti[s];
   const uint64_t kick = g.kick;
-  unsigned int status = g.status[s];
+  // status bits raised in this chunk; or-ed into the system's word at the end
+  // (the transit searches and the consumer of the previous chunk may be
+  // or-ing theirs in meanwhile)
+  unsigned int status = 0;
   for (int kk = 0; kk < g.K; kk++) {
     const long long istep = k0 + kk;
     if (istep >= nst) break;
@@ -121,7 +124,8 @@ __global__ void __launch_bounds__(PROD_BS * PROD_MAX_WARPS) orbit_chunk_kernel(G
     g.gsave[q * S + s] = gsave[q];
     g.count[q * S + s] = count[q];
   }
-  g.status[s] = status;
+  if (!state_finite<N>(st)) status |= NBG_STATUS_NONFINITE;
+  if (status) atomicOr(g.status + s, status);
 }
 
 
@@ -390,10 +394,13 @@ __global__ void __launch_bounds__(CONS_BS) jacobian_chunk_kernel(GroupArgs g, in
   }
   double* Jw = g.Jint + (size_t)s * R6 * M + c;
   double* Ew = g.Eint + (size_t)s * R6 * M + c;
+  bool finite = true;
   for (int r = 0; r < R6; r++) {
     Jw[(size_t)r * M] = J[r * CONS_BS];
     Ew[(size_t)r * M] = E[r * CONS_BS];
+    finite = finite && isfinite(J[r * CONS_BS]);
   }
+  if (!finite) atomicOr(g.status + s, NBG_STATUS_NONFINITE);
 }
 
 // gsave[i] = g!(i, ti, x, v) for every occultor (Transits.jl:146-149).

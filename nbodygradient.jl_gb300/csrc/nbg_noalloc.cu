@@ -10,36 +10,35 @@
 // Jacobian columns) is carved out of the one array below, whose size is fixed
 // when the library is built (NBG_NOALLOC_SCRATCH_BYTES in nbg.h).
 //
-// The array lives in this translation unit alone, so its device memory is
-// reserved only once something asks for its address, not by the other
-// entry points.
+// When the array's device memory is reserved depends on CUDA's module
+// loading.  With lazy loading (the default since CUDA 12.2) the module that
+// holds the array is loaded on a device -- and its 64 MiB reserved there --
+// the first time the array's address is asked for on that device, i.e. by
+// the first call of the entry point; a caller that then holds the rest of
+// the GPU's memory must make that first call before taking it, or the lookup
+// fails with an out-of-memory error (reported as NBG_ECUDA).  With
+// CUDA_MODULE_LOADING=EAGER every context that loads the library reserves the
+// array when it is created, whether or not it ever calls the entry point.
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 #include "../../include/nbg.h"
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NBG_NOALLOC_SCRATCH_BYTES];
 
-namespace {
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mutex;
-unsigned char* g_scratch_ptr[kMaxDevices] = {};
-}  // namespace
-
-// Device address of the scratch array on `device`, which must be the current
-// device.  Resolved with cudaGetSymbolAddress on the first request for each
-// device and cached; later requests only read the cache.
+// Device address of the scratch array on the current device, which must be
+// `device`.  Looked up with cudaGetSymbolAddress on every call (cheap once the
+// module is loaded), so that an address never outlives the CUDA context it
+// belongs to: a cache keyed by device would hand out a stale pointer after the
+// host process resets the device and a new primary context is created.
 __attribute__((visibility("hidden"))) cudaError_t nbg_noalloc_scratch(int device, unsigned char** out) {
   *out = nullptr;
-  if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (!g_scratch_ptr[device]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_scratch_ptr[device] = (unsigned char*)p;
-  }
-  *out = g_scratch_ptr[device];
+  int cur = -1;
+  cudaError_t e = cudaGetDevice(&cur);
+  if (e != cudaSuccess) return e;
+  if (cur != device) return cudaErrorInvalidDevice;
+  void* p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return e;
+  *out = (unsigned char*)p;
   return cudaSuccess;
 }

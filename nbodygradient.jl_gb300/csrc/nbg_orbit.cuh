@@ -38,6 +38,16 @@ struct Sys {
   double dqdt[7 * N];
 };
 
+// x and v all finite (the State check of Integrator.jl:137-143, which the
+// reference only prints; here it raises NBG_STATUS_NONFINITE).
+template <int N>
+__device__ __forceinline__ bool state_finite(const Sys<N>& st) {
+  bool ok = true;
+#pragma unroll
+  for (int q = 0; q < 3 * N; q++) ok = ok && isfinite(st.x[q]) && isfinite(st.v[q]);
+  return ok;
+}
+
 // Scratch of one step (the Derivatives fields the producer needs,
 // src/PreAllocArrays.jl:65-113), compact layouts.
 template <int N>

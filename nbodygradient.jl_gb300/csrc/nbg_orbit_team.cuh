@@ -248,6 +248,7 @@ __global__ void __launch_bounds__(PROD_BS * PROD_MAX_WARPS) orbit_team_kernel(Gr
       g.gsave[q * S + s] = gsv[tm][q];
       g.count[q * S + s] = cnt[tm][q];
     }
+    if (t == 0 && !state_finite<N>(st)) atomicOr(g.status + s, NBG_STATUS_NONFINITE);
   }
 }
 

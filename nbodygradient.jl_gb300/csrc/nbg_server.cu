@@ -40,6 +40,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -110,6 +111,23 @@ __global__ void deactivate_kernel(int n, const int* list, int* sysidx, long long
   }
 }
 
+// Cancellation of running requests (nbg_server_cancel), on the producer
+// stream before chunk `first / K` is produced: the slot's step count is cut to
+// the steps already run, so that this chunk's and every later chunk's kernels
+// skip the slot (the producer queues no transit search for it) while the
+// slot keeps its sysidx until its retirement on the consumer stream, as a
+// finished request does.  Kernels of the previous chunk that read the cut
+// count run fewer steps of a request whose results are discarded.
+__global__ void truncate_kernel(int n, const int* list, long long* nsteps, const long long* kbase, long long first) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const int s = list[i];
+    long long done = first - kbase[s];
+    if (done < 0) done = 0;
+    if (nsteps[s] > done) nsteps[s] = done;
+  }
+}
+
 // Per-slot staging layout (doubles) of a request in the caller's layout:
 // x, v, xerror, verror (3N each), m (N), dqdt (7N), count (N int64) and,
 // with grad, jac_step, jac_error, jac_init (M^2 each).
@@ -143,11 +161,15 @@ struct Request {
   std::string msg;  // error message of a failed request
   uint32_t status = 0;
   bool released = false;
+  // nbg_server_cancel: set under the server mutex; read by the server thread
+  std::atomic<bool> cancel{false};
+  bool retiring = false;  // its last chunk and retirement are queued (under the mutex)
 };
 
 struct Inflight {
   cudaEvent_t ev;
   std::vector<Request*> retired;
+  std::vector<Request*> cancelled;  // running requests retired early by nbg_server_cancel
 };
 
 struct Group {
@@ -165,6 +187,7 @@ struct Group {
   int* d_bad = nullptr;
   AdmitRec* d_admit = nullptr;
   int* d_list = nullptr;
+  int* d_list_c = nullptr;  // slots of cancelled requests (producer stream)
   unsigned char* ring = nullptr;  // pinned upload ring: entries of [C AdmitRec][C int]
   size_t ring_entry = 0;
   std::vector<cudaEvent_t> events;  // chunk completion, ring of max_inflight + 1
@@ -240,6 +263,10 @@ struct nbg_server {
   int fail_rc = NBG_OK;
   std::string fail_msg;
   nbg_server_stats_t stats;
+  // threads inside nbg_server_wait_any / nbg_server_poll; nbg_server_stop
+  // waits for them to leave before it frees anything they use
+  int clients = 0;
+  bool closing = false;  // the server thread has exited: waits end
   // server thread only
   std::vector<Group*> groups;
   std::map<std::tuple<int, int, unsigned long long>, int> group_of;
@@ -259,6 +286,21 @@ struct nbg_server {
 };
 
 namespace {
+
+// Registers a thread inside nbg_server_wait_any / nbg_server_poll for its
+// whole call (the poll's copies run outside the mutex).
+struct ClientGuard {
+  nbg_server* srv;
+  explicit ClientGuard(nbg_server* s) : srv(s) {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    srv->clients++;
+  }
+  ~ClientGuard() {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    srv->clients--;
+    srv->cv_done.notify_all();
+  }
+};
 
 // Device buffers of a group; charged against the server's budget.
 int create_group(nbg_server* srv, int N, int grad, unsigned long long kick, Group** out) {
@@ -307,7 +349,7 @@ int create_group(nbg_server* srv, int N, int grad, unsigned long long kick, Grou
   }
   want(&G->stage, S * G->lay.stride);
   want(&G->d_off, S); want(&G->d_kbase, S); want(&G->d_offtt, S); want(&G->d_offdq, S);
-  want(&G->d_mask, S); want(&G->d_mask_r, S); want(&G->d_bad, 1); want(&G->d_admit, S); want(&G->d_list, S);
+  want(&G->d_mask, S); want(&G->d_mask_r, S); want(&G->d_bad, 1); want(&G->d_admit, S); want(&G->d_list, S); want(&G->d_list_c, S);
   size_t total = 0;
   for (auto& it : items) total += (it.bytes + 255) / 256 * 256;
   if (srv->group_bytes + total > srv->cfg.hbm_budget_bytes / 2) {
@@ -434,8 +476,27 @@ int service_group(nbg_server* srv, int gi) {
       r->status = st32;
       finish(srv, r, NBG_OK);
     }
+    for (Request* r : f.cancelled) {
+      srv->arena.release(r->heap_off, r->heap_n);
+      finish(srv, r, NBG_ECANCELLED, "cancelled while running; its slot was retired at a chunk boundary");
+    }
     srv->stats.hbm_outputs_in_use = srv->arena.used * sizeof(double);
-    if (!f.retired.empty()) srv->cv_done.notify_all();
+    if (!f.retired.empty() || !f.cancelled.empty()) srv->cv_done.notify_all();
+  }
+  // ---- cancelled requests still waiting for a slot leave the queue
+  if (!G->pending.empty()) {
+    bool any = false;
+    for (Request* r : G->pending) any = any || r->cancel.load(std::memory_order_relaxed);
+    if (any) {
+      std::lock_guard<std::mutex> lk(srv->mu);
+      std::deque<Request*> keep;
+      for (Request* r : G->pending) {
+        if (r->cancel.load()) finish(srv, r, NBG_ECANCELLED, "cancelled before it was admitted");
+        else keep.push_back(r);
+      }
+      G->pending.swap(keep);
+      srv->cv_done.notify_all();
+    }
   }
   if ((int)G->inflight.size() >= D) return 0;
   // ---- admission (host decisions; a slot's previous occupant, if any, was
@@ -522,6 +583,34 @@ int service_group(nbg_server* srv, int gi) {
     launch_group_seed(N, gm, st);
     launches++;
   }
+  // ---- which slots this chunk retires: those whose last step it runs, and
+  // those of cancelled requests (cut to the steps already run, below).
+  // Decided under the mutex, so that nbg_server_cancel sees either a request
+  // whose retirement is queued (too late to cancel) or one that a chunk not
+  // yet produced will retire as cancelled.
+  Inflight f;
+  f.ev = G->events[e];
+  int nr = 0, nc = 0;
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    for (int s = 0; s < C; s++) {
+      Request* r = G->slot_req[s];
+      if (!r) continue;
+      if (r->cancel.load()) {
+        f.cancelled.push_back(r);
+      } else if (r->c_end == c) {
+        r->retiring = true;
+        ulist[nr++] = s;
+        f.retired.push_back(r);
+      }
+    }
+  }
+  for (Request* r : f.cancelled) ulist[nr + nc++] = r->slot;  // deactivated, not copied out
+  if (nc) {
+    NBG_CUDA(cudaMemcpyAsync(G->d_list_c, ulist + nr, sizeof(int) * nc, cudaMemcpyHostToDevice, st));
+    truncate_kernel<<<(nc + 127) / 128, 128, 0, st>>>(nc, G->d_list_c, g.nsteps, G->d_kbase, c * K);
+    launches++;
+  }
   // ---- one chunk of every active slot: the producer on st, then the
   // searches on stt beside the operator records on sw, then the consumer
   NBG_CUDA(cudaMemsetAsync(gc.task_count, 0, sizeof(int), st));
@@ -542,20 +631,13 @@ int service_group(nbg_server* srv, int gi) {
     if ((rc = launch_group_jacobian(N, gc, (int)c, sw))) return rc;
     launches += 1;
   }
-  // ---- retirement of the slots whose last step ran in this chunk
-  Inflight f;
-  f.ev = G->events[e];
-  int nr = 0;
-  for (int s = 0; s < C; s++) {
-    Request* r = G->slot_req[s];
-    if (r && r->c_end == c) {
-      ulist[nr++] = s;
-      f.retired.push_back(r);
-    }
+  // ---- retirement of the slots whose last step ran in this chunk, and of
+  // the cancelled ones
+  if (nr + nc) {
+    // on the consumer stream, after the chunk's consumer and searches
+    NBG_CUDA(cudaMemcpyAsync(G->d_list, ulist, sizeof(int) * (nr + nc), cudaMemcpyHostToDevice, sw));
   }
   if (nr) {
-    // on the consumer stream, after the chunk's consumer and searches
-    NBG_CUDA(cudaMemcpyAsync(G->d_list, ulist, sizeof(int) * nr, cudaMemcpyHostToDevice, sw));
     NBG_CUDA(cudaMemsetAsync(G->d_mask_r, 0xff, sizeof(int) * C, sw));
     mark_kernel<<<(nr + 127) / 128, 128, 0, sw>>>(nr, G->d_list, G->d_mask_r);
     double* sg = G->stage;
@@ -568,8 +650,15 @@ int service_group(nbg_server* srv, int gi) {
                          true, sw);
       launches += 2;
     }
-    deactivate_kernel<<<(nr + 127) / 128, 128, 0, sw>>>(nr, G->d_list, g.sysidx, G->d_kbase);
+  }
+  if (nr + nc) {
+    deactivate_kernel<<<(nr + nc + 127) / 128, 128, 0, sw>>>(nr + nc, G->d_list, g.sysidx, G->d_kbase);
     launches++;
+    for (Request* r : f.cancelled) {
+      G->slot_req[r->slot] = nullptr;
+      G->free_at[r->slot] = c + 2;
+      G->active--;
+    }
     for (Request* r : f.retired) {
       NBG_CUDA(cudaMemcpyAsync(r->host, G->stage + (size_t)r->slot * stride, sizeof(double) * stride,
                                cudaMemcpyDeviceToHost, sw));
@@ -614,6 +703,12 @@ void server_main(nbg_server* srv) {
       stopping = srv->stop;
     }
     for (Request* r : in) {
+      if (r->cancel.load()) {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        finish(srv, r, NBG_ECANCELLED, "cancelled before it was admitted");
+        srv->cv_done.notify_all();
+        continue;
+      }
       auto key = std::make_tuple((int)r->d.n, (int)r->d.grad, r->kick);
       auto it = srv->group_of.find(key);
       int gi;
@@ -818,6 +913,7 @@ int nbg_server_enqueue(nbg_server* srv, const nbg_system_desc* desc, double t0, 
 
 int nbg_server_wait_any(nbg_server* srv, int32_t timeout_ms, int64_t* id) {
   if (!srv || !id) return set_error(NBG_EINVAL, "NULL argument");
+  ClientGuard guard(srv);
   std::unique_lock<std::mutex> lk(srv->mu);
   auto pred = [&] {
     while (!srv->done_ids.empty()) {
@@ -825,12 +921,15 @@ int nbg_server_wait_any(nbg_server* srv, int32_t timeout_ms, int64_t* id) {
       if (it != srv->reqs.end() && !it->second->released) return true;
       srv->done_ids.pop_front();  // already collected by nbg_server_poll
     }
-    return srv->fail_rc != NBG_OK;
+    return srv->fail_rc != NBG_OK || srv->closing;
   };
   if (timeout_ms < 0) srv->cv_done.wait(lk, pred);
   else if (!srv->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred))
     return set_error(NBG_ETIMEOUT, "no request completed within %d ms", timeout_ms);
-  if (srv->done_ids.empty()) return set_error(srv->fail_rc, "server failed: %s", srv->fail_msg.c_str());
+  if (srv->done_ids.empty()) {
+    if (srv->fail_rc != NBG_OK) return set_error(srv->fail_rc, "server failed: %s", srv->fail_msg.c_str());
+    return set_error(NBG_ECANCELLED, "server stopped with no completed request left to collect");
+  }
   *id = srv->done_ids.front();
   srv->done_ids.pop_front();
   return NBG_OK;
@@ -840,6 +939,7 @@ int nbg_server_poll(nbg_server* srv, int64_t id, int32_t timeout_ms, double* t, 
                     double* xerror, double* verror, double* jac_step, double* jac_error, double* dqdt, double* tt,
                     double* dtdq0, double* dtdelements, int64_t* count, nbg_request_info* info) {
   if (!srv) return set_error(NBG_EINVAL, "srv is NULL");
+  ClientGuard guard(srv);
   Request* r;
   {
     std::unique_lock<std::mutex> lk(srv->mu);
@@ -900,6 +1000,22 @@ int nbg_server_poll(nbg_server* srv, int64_t id, int32_t timeout_ms, double* t, 
   return NBG_OK;
 }
 
+int nbg_server_cancel(nbg_server* srv, int64_t id) {
+  if (!srv) return set_error(NBG_EINVAL, "srv is NULL");
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    auto it = srv->reqs.find(id);
+    if (it == srv->reqs.end()) return set_error(NBG_EINVAL, "unknown request id %lld", (long long)id);
+    Request* r = it->second;
+    if (r->state == REQ_DONE || r->state == REQ_FAILED || r->retiring)
+      return set_error(NBG_EINVAL, "request %lld has already finished or is being retired: its result stands",
+                       (long long)id);
+    r->cancel.store(true);
+  }
+  srv->cv_work.notify_one();
+  return NBG_OK;
+}
+
 int nbg_server_stats(nbg_server* srv, nbg_server_stats_t* out) {
   if (!srv || !out) return set_error(NBG_EINVAL, "NULL argument");
   std::lock_guard<std::mutex> lk(srv->mu);
@@ -915,6 +1031,14 @@ int nbg_server_stop(nbg_server* srv) {
   }
   srv->cv_work.notify_all();
   if (srv->thread.joinable()) srv->thread.join();
+  {
+    // every request has reached its end (admitted ones ran to completion,
+    // the others were cancelled): let the threads collecting them finish
+    std::unique_lock<std::mutex> lk(srv->mu);
+    srv->closing = true;
+    srv->cv_done.notify_all();
+    srv->cv_done.wait(lk, [&] { return srv->clients == 0; });
+  }
   cudaSetDevice(srv->device);
   for (Group* G : srv->groups) destroy_group(G);
   srv->groups.clear();

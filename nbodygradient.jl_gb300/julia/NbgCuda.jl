@@ -39,6 +39,17 @@ function last_error()
     return unsafe_string(pointer(buf))
 end
 
+const NBG_ENONFINITE = -5
+
+# A non-zero return code becomes an error, except NBG_ENONFINITE: the
+# reference lets non-finite values propagate into the State silently, so the
+# shim keeps the call's (written) outputs and only warns.
+function check_rc(rc)
+    rc == 0 && return
+    rc == NBG_ENONFINITE && (@warn "libnbg_cuda: " * last_error(); return)
+    error("libnbg_cuda: ", last_error())
+end
+
 function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, tt::TransitTiming{Float64};
                                                     grad::Bool=true, return_arrays::Bool=false)
     t = s.t  # Vector{Float64} of length 1, updated in place
@@ -53,8 +64,10 @@ function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, tt::Trans
                    s.jac_step, s.jac_error, s.dqdt, s.pair, s.jac_init, tt.ntt,
                    tt.tt, tt.dtdq0, tt.dtdelements, tt.count)
     end
-    rc == 0 || error("libnbg_cuda: ", last_error())
-    return_arrays && return nothing  # no Derivatives scratch exists on this path
+    check_rc(rc)
+    # the step scratch for later three-argument calls (Transits.jl:176-178); this
+    # path keeps its scratch on the device, so a fresh one is handed back
+    return_arrays && return NbodyGradient.Derivatives(Float64, s.n)
     return nothing
 end
 
@@ -71,7 +84,8 @@ function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, ttbv::Tra
                    s.jac_step, s.jac_error, s.dqdt, s.pair, s.jac_init, ttbv.ntt,
                    ttbv.ttbv, ttbv.dtbvdq0, ttbv.dtbvdelements, ttbv.count)
     end
-    rc == 0 || error("libnbg_cuda: ", last_error())
+    check_rc(rc)
+    return_arrays && return NbodyGradient.Derivatives(Float64, s.n)
     return nothing
 end
 
@@ -99,7 +113,7 @@ function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, time::Flo
                    context(), s.n, intr.h, time, grad ? 1 : 0,
                    s.t, s.x, s.v, s.m, s.xerror, s.verror, s.jac_step, s.jac_error, s.dqdt, s.pair)
     end
-    rc == 0 || error("libnbg_cuda: ", last_error())
+    check_rc(rc)
     return
 end
 
@@ -112,7 +126,7 @@ function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, N::Int64;
                    context(), s.n, intr.h, N, grad ? 1 : 0,
                    s.t, s.x, s.v, s.m, s.xerror, s.verror, s.jac_step, s.jac_error, s.dqdt, s.pair)
     end
-    rc == 0 || error("libnbg_cuda: ", last_error())
+    check_rc(rc)
     intr.h < 0 && (intr.h = -intr.h)  # as the reference leaves it (Integrator.jl:228-229)
     return
 end
@@ -133,7 +147,7 @@ function (intr::Integrator{Float64,typeof(ahl21!)})(s::State{Float64}, o::Cartes
                    s.t, s.x, s.v, s.m, s.xerror, s.verror, s.jac_step, s.jac_error, s.dqdt, s.pair,
                    ts, xs, vs, js)
     end
-    rc == 0 || error("libnbg_cuda: ", last_error())
+    check_rc(rc)
     for i in 1:nstep  # o.states[i] = the state before step i (Outputs.jl:38-40)
         si = deepcopy(s)
         si.t[1] = ts[i]; si.x .= xs[:, :, i]; si.v .= vs[:, :, i]; si.jac_step .= js[:, :, i]

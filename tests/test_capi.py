@@ -86,6 +86,7 @@ def test_new_entry_points_reject_null_arguments_without_a_gpu():
     assert L.nbg_server_enqueue(None, None, 0.0, *([None] * 10), None) == E
     assert L.nbg_server_stats(None, None) == E
     assert L.nbg_server_stop(None) == nbg._lib.NBG_OK
+    assert L.nbg_server_cancel(None, 1) == E
 
 
 def test_transit_parameters_and_cartesian_output_shapes():

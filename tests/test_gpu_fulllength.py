@@ -98,6 +98,54 @@ def _compare_system(b, q, so, to, tmax):
             "dtdelements": r_de}
 
 
+def _excess(gpu, ref, count, dtdq0=None, jac_init=None):
+    """Entries of a transit-derivative array beyond the tests/parity.py tolerance: (entries checked,
+    entries beyond, worst ratio, largest |entry| / row scale among those beyond)."""
+    n, ntt = gpu.shape[0], gpu.shape[1]
+    checked = beyond = 0
+    worst = big = 0.0
+    for j, c in enumerate(count):
+        for t in range(min(int(c), ntt)):
+            r, g = ref[j, t], gpu[j, t]
+            s = float(np.max(np.abs(r)))
+            if s == 0.0:
+                continue
+            mag = np.abs(r)
+            if dtdq0 is not None:
+                mag = mag + (np.abs(dtdq0[j, t]).ravel(order="F") @ np.abs(jac_init)).reshape((7, n), order="F")
+            ratio = np.abs(g - r) / (P.DT_RTOL * (mag + P.DT_FLOOR * s))
+            checked += ratio.size
+            over = ratio > 1.0
+            beyond += int(np.count_nonzero(over))
+            worst = max(worst, float(np.max(ratio)))
+            if over.any():
+                big = max(big, float(np.max(np.abs(r[over]))) / s)
+    return checked, beyond, worst, big
+
+
+def _failure_stats(b, q, so, to):
+    n, ntt = int(b.n[q]), int(b.ntt[q])
+    g_dq = b.view("dtdq0", q).reshape((n, ntt, 7, n), order="F")
+    g_de = b.view("dtdelements", q).reshape((n, ntt, 7, n), order="F")
+    a = _excess(g_dq, to.dtdq0, to.count)
+    e = _excess(g_de, to.dtdelements, to.count, to.dtdq0, so.jac_init)
+    return ("dtdq0: %d of %d entries beyond, worst %.3g x, largest such entry %.2g of its row scale; "
+            "dtdelements: %d of %d beyond, worst %.3g x, largest %.2g of its row scale" % (a[1], a[0], a[2], a[3],
+                                                                                         e[1], e[0], e[2], e[3]))
+
+
+def _dump(name, q, b, so, to):
+    """Both sides of a failing system, for offline study (NBG_PARITY_DUMP: a directory)."""
+    d = os.environ.get("NBG_PARITY_DUMP")
+    if not d:
+        return
+    os.makedirs(d, exist_ok=True)
+    arr = {"gpu_" + k: b.view(k, q) for k in ("x", "v", "tt", "dtdq0", "dtdelements", "count", "jac_step")}
+    arr.update(ref_x=so.x, ref_v=so.v, ref_tt=to.tt, ref_dtdq0=to.dtdq0, ref_dtdelements=to.dtdelements,
+               ref_count=to.count, ref_jac_step=so.jac_step, jac_init=so.jac_init)
+    np.savez_compressed(os.path.join(d, "%s_system%d.npz" % (name, q)), **arr)
+
+
 def _run_and_compare(name, states, hs, tms, ntts, sample):
     jobs = [(states[q], hs[q], tms[q], ntts[q]) for q in sample]
     runs = _oracle_runs(jobs)
@@ -106,13 +154,20 @@ def _run_and_compare(name, states, hs, tms, ntts, sample):
     bad = nbg._lib.NBG_STATUS_NONFINITE | nbg._lib.NBG_STATUS_NTT_OVERFLOW
     assert np.all((b.status & bad) == 0)
     results = runs.result()
-    rows = []
+    rows, failures = [], []
     for q, (so, to) in zip(sample, results):
-        r = _compare_system(b, q, so, to, tms[q])
+        try:
+            r = _compare_system(b, q, so, to, tms[q])
+        except AssertionError as e:
+            failures.append("system %d (n = %d, %d steps): %s [%s]" % (q, int(b.n[q]), abs(round(tms[q] / hs[q])), e,
+                                                                        _failure_stats(b, q, so, to)))
+            _dump(name, q, b, so, to)
+            continue
         r.update(system=int(q), steps=int(abs(round(tms[q] / hs[q]))))
         rows.append(r)
-    worst = {k: max(r[k] for r in rows) for k in ("tt", "dtdq0", "dtdelements")}
-    _report(name, systems=len(states), sample=len(sample), worst=worst, rows=rows)
+    worst = {k: max([r[k] for r in rows] or [0.0]) for k in ("tt", "dtdq0", "dtdelements")}
+    _report(name, systems=len(states), sample=len(sample), worst=worst, rows=rows, failures=failures)
+    assert not failures, "\n".join(failures)
     return worst
 
 

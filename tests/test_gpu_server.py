@@ -162,7 +162,8 @@ def test_full_length_requests_and_latency_record():
     assert_same((s, tt), (s1, tt1))
 
 
-def test_errors_and_cancellation():
+def test_request_argument_errors():
+    """Malformed requests are rejected at enqueue; unknown ids and empty waits report their own codes."""
     with nbg.Server(slots_per_group=32) as srv:
         el, h, tmax = W.plain_3body(1)
         ic = W.ic_of(el)
@@ -171,8 +172,152 @@ def test_errors_and_cancellation():
         tt.count[0] = 1
         with pytest.raises(ValueError):
             srv.submit(s, tt, nbg.Integrator(nbg.ahl21, h, 0.0, tmax))
-        with pytest.raises(nbg.NbgError):
+        with pytest.raises(nbg.NbgError) as ei:
             srv.result(123456, s, tt, timeout_ms=0)
+        assert ei.value.code == nbg._lib.NBG_EINVAL
         with pytest.raises(nbg.NbgError) as ei:
             srv.wait_any(timeout_ms=10)
         assert ei.value.code == nbg._lib.NBG_ETIMEOUT
+        with pytest.raises(nbg.NbgError) as ei:
+            srv.cancel(123456)
+        assert ei.value.code == nbg._lib.NBG_EINVAL
+
+
+def _long_3body(nreq, seed, steps=2000):
+    """nreq 3-body gradient requests of `steps` steps (one group)."""
+    els, hs, _ = W.batch_uneven(nreq, seed=seed, nmin=3, nmax=3)
+    out = []
+    for el, h in zip(els, hs):
+        ic = W.ic_of(el)
+        tmax = float(h * steps)
+        out.append((nbg.State(ic), nbg.TransitTiming(tmax, ic), nbg.Integrator(nbg.ahl21, h, 0.0, tmax), True))
+    return out
+
+
+def _wait_admitted(srv, n, timeout_s=60.0):
+    t0 = time.time()
+    while srv.stats()["admitted"] < n:
+        assert time.time() - t0 < timeout_s, srv.stats()
+        time.sleep(0.002)
+
+
+def _alone(req):
+    s, tt, intr, grad = fresh(req)
+    intr(s, tt, grad=grad)
+    return s, tt
+
+
+def test_cancel_waiting_and_running_requests():
+    """32 slots hold 32 long requests; of 4 more that wait for a slot one is cancelled while waiting, and
+    one of the running requests is cancelled mid-integration.  Both report NBG_ECANCELLED; every other
+    request completes bitwise as alone, including the one admitted into the cancelled request's slot;
+    cancelling a request that has finished is refused and leaves its result intact."""
+    reqs = _long_3body(36, seed=51)
+    with nbg.Server(slots_per_group=32, chunk_steps=8) as srv:
+        outs = [fresh(r) for r in reqs]
+        ids = [srv.submit(s, tt, intr, grad) for s, tt, intr, grad in outs]
+        _wait_admitted(srv, 32)
+        assert srv.stats()["pending"] == 4
+        srv.cancel(ids[33])  # waiting for a slot
+        srv.cancel(ids[5])   # running
+        for q in (5, 33):
+            s, tt, _, _ = outs[q]
+            with pytest.raises(nbg.NbgError) as ei:
+                srv.result(ids[q], s, tt, timeout_ms=120000)
+            assert ei.value.code == nbg._lib.NBG_ECANCELLED
+        infos = {}
+        for q in range(36):
+            if q in (5, 33):
+                continue
+            s, tt, _, _ = outs[q]
+            infos[q] = srv.result(ids[q], s, tt, timeout_ms=120000)
+        st = srv.stats()
+        assert st["completed"] == 34 and st["failed"] == 2 and st["running"] == 0 and st["pending"] == 0
+        # a finished request cannot be cancelled: the refusal leaves it collectable
+        s, tt, intr, grad = fresh(reqs[0])
+        rid = srv.submit(s, tt, intr, grad)
+        srv.result(rid, s, tt, timeout_ms=120000)
+        with pytest.raises(nbg.NbgError) as ei:
+            srv.cancel(rid)
+        assert ei.value.code == nbg._lib.NBG_EINVAL
+    for q in (0, 6, 31, 32, 34, 35):
+        assert_same((outs[q][0], outs[q][1]), _alone(reqs[q]))
+
+
+def test_stop_cancels_requests_not_yet_admitted():
+    """nbg_server_stop with requests still waiting for a slot: threads collecting them get
+    NBG_ECANCELLED, the running requests run to completion, and stop returns cleanly."""
+    reqs = _long_3body(35, seed=52)
+    srv = nbg.Server(slots_per_group=32, chunk_steps=8)
+    outs = [fresh(r) for r in reqs]
+    ids = [srv.submit(s, tt, intr, grad) for s, tt, intr, grad in outs]
+    _wait_admitted(srv, 32)
+    codes = {}
+
+    def collect(q):
+        s, tt, _, _ = outs[q]
+        try:
+            srv.result(ids[q], s, tt, timeout_ms=120000)
+            codes[q] = 0
+        except nbg.NbgError as e:
+            codes[q] = e.code
+
+    threads = [threading.Thread(target=collect, args=(q,)) for q in (32, 33, 34)]
+    for t in threads:
+        t.start()
+    time.sleep(0.05)
+    srv.stop()
+    for t in threads:
+        t.join(timeout=60)
+    assert codes == {32: nbg._lib.NBG_ECANCELLED, 33: nbg._lib.NBG_ECANCELLED, 34: nbg._lib.NBG_ECANCELLED}
+
+
+def test_output_arena_too_small_requests_wait_then_complete():
+    """An HBM budget whose output half holds one request's outputs at a time (transit arrays of
+    ntt = 20000): four requests are admitted one after another, each waiting for the previous one's
+    outputs to be released, and all complete bitwise as alone."""
+    els, hs, _ = W.batch_uneven(4, seed=53, nmin=3, nmax=3)
+    big = []
+    for el, h in zip(els, hs):
+        ic = W.ic_of(el)
+        tmax = float(h * 400)
+        big.append((nbg.State(ic), nbg.TransitTiming(tmax, ic, ntt=20000), nbg.Integrator(nbg.ahl21, h, 0.0, tmax),
+                    True))
+    # the group's slot buffers, measured on a server with room to spare
+    with nbg.Server(slots_per_group=32, chunk_steps=8) as probe:
+        s, tt, intr, grad = fresh(big[0])
+        probe.result(probe.submit(s, tt, intr, grad), s, tt, timeout_ms=120000)
+        group_bytes = probe.stats()["hbm_groups"]
+    out_bytes = 8 * (3 * 20000 + 2 * 7 * 9 * 20000)  # tt, dtdq0, dtdelements of one request
+    half = max(group_bytes, int(1.5 * out_bytes))
+    with nbg.Server(slots_per_group=32, chunk_steps=8, hbm_budget_bytes=2 * half) as srv:
+        outs = [fresh(r) for r in big]
+        ids = [srv.submit(s, tt, intr, grad) for s, tt, intr, grad in outs]
+        infos = [srv.result(i, o[0], o[1], timeout_ms=120000) for i, o in zip(ids, outs)]
+    assert all(i["rc"] == 0 for i in infos)
+    runs = sorted(infos, key=lambda i: i["queue_ms"])
+    # one at a time: each later request waited at least most of an earlier one's run
+    for k in range(1, 4):
+        assert runs[k]["queue_ms"] >= 0.5 * runs[k - 1]["run_ms"], [(i["queue_ms"], i["run_ms"]) for i in runs]
+    for q in range(4):
+        assert_same((outs[q][0], outs[q][1]), _alone(big[q]))
+
+
+def test_group_larger_than_budget_fails_with_enomem():
+    """A 2 MB budget: a 3-body gradient group's slot buffers (its two halves of operator records alone
+    take 2 MB) do not fit the 1 MB group half, so the request fails NBG_ENOMEM; a gradient-free group
+    fits, but a request whose outputs (ntt = 60000: 1.4 MB) exceed the 1 MB output arena fails the same
+    way; the server keeps serving and counts both failures."""
+    with nbg.Server(slots_per_group=32, chunk_steps=8, hbm_budget_bytes=2 * 1024 * 1024) as srv:
+        s, tt, intr, grad = fresh(_long_3body(1, seed=54, steps=100)[0])
+        with pytest.raises(nbg.NbgError) as ei:
+            srv.result(srv.submit(s, tt, intr, grad), s, tt, timeout_ms=120000)
+        assert ei.value.code == nbg._lib.NBG_ENOMEM
+        el, h, _ = W.plain_3body(2)
+        ic = W.ic_of(el)
+        s2, tt2 = nbg.State(ic), nbg.TransitTiming(10 * h, ic, ntt=60000)
+        with pytest.raises(nbg.NbgError) as ei:
+            srv.result(srv.submit(s2, tt2, nbg.Integrator(nbg.ahl21, h, 0.0, 10 * h), False), s2, tt2,
+                       timeout_ms=120000)
+        assert ei.value.code == nbg._lib.NBG_ENOMEM
+        assert srv.stats()["failed"] == 2

@@ -91,6 +91,36 @@ def test_noalloc_matches_pooled_entry_point_twice():
         _compare(b, tms, got, ref)
 
 
+def test_noalloc_repeat_call_leaves_device_memory_unchanged():
+    """After the first call on the device (which, under lazy module loading, reserves the fixed
+    scratch array), a call changes the device's free memory by not one byte."""
+    import torch
+    ctx = nbg.Context(0)
+    b, _ = _batch()
+    dev = {k: torch.from_numpy(a.copy()).cuda() for k, a in b.arrays.items()}
+    b.run_device_noalloc(dev, ctx)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    b.run_device_noalloc(dev, ctx)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+
+
+def test_noalloc_shrinks_its_chunk_to_fit():
+    """With the context's chunk set to 4096 steps the working set cannot fit the 64 MiB scratch
+    (the operator records of one 2-body gradient group alone take 4096 x 172 x 32 doubles =
+    180 MB), so the call shortens its chunk; results still match the pooled entry point."""
+    ctx = nbg.Context(0)
+    ctx.set_tuning(chunk_steps=4096)
+    ref_ctx = nbg.Context(0)
+    b, tms = _batch()
+    ref, ref_status = _run(b, lambda dev: b.run_device(dev, ref_ctx))
+    got, status = _run(b, lambda dev: b.run_device_noalloc(dev, ctx))
+    assert np.array_equal(status, ref_status)
+    _compare(b, tms, got, ref)
+
+
 def test_noalloc_rejects_too_many_systems():
     ctx = nbg.Context(0)
     L = nbg._lib.load()
