@@ -197,6 +197,47 @@ def cpu_baseline(nbg, states, timings, hs, tms, nsteps, target_s=12.0, nthreads=
     return total_ss / total_t, nthreads, used, total_t
 
 
+def cpu_rate_by_n(nbg, workload, seed, target_s=6.0, cap_steps=1500, nthreads=None):
+    """The oracle's system-steps/s on a workload of mixed body counts: per body count, a sample of its
+    systems integrated for their first min(nsteps, cap_steps) steps, one system per host thread, for about
+    target_s of wall time; the rates are combined as the time the whole workload would take at them."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as O
+    from concurrent.futures import ThreadPoolExecutor
+    O.build()
+    nthreads = nthreads or os.cpu_count() or 1
+    states, timings, hs, tms, nsteps = build_workload(nbg, workload, None, seed)
+    by_n = {}
+    for q, st in enumerate(states):
+        by_n.setdefault(st.n, []).append(q)
+    rates, total_t = {}, 0.0
+
+    def one(q):
+        s = states[q]
+        so = O.OState(s.x, s.v, s.m, jac_init=s.jac_init)
+        k = min(nsteps[q], cap_steps)
+        tm = k * hs[q]
+        to = O.OTiming(s.n, timings[q].ntt, 0)
+        O.integrate_transits(so, to, hs[q], tm)
+        return k
+
+    for n, qs in sorted(by_n.items()):
+        done, t_used, used = 0, 0.0, 0
+        batch = nthreads
+        while t_used < target_s / len(by_n) and used < len(qs):
+            pick = [qs[(used + r) % len(qs)] for r in range(batch)]
+            used += batch
+            t0 = time.perf_counter()
+            with ThreadPoolExecutor(max_workers=nthreads) as ex:
+                done += sum(ex.map(one, pick))
+            t_used += time.perf_counter() - t0
+        rates[n] = done / t_used
+        total_t += t_used
+    steps_n = {n: sum(nsteps[q] for q in qs) for n, qs in by_n.items()}
+    value = sum(steps_n.values()) / sum(steps_n[n] / rates[n] for n in steps_n)
+    return value, {str(n): r for n, r in rates.items()}, nthreads, total_t
+
+
 def replica_seed(seed, rank):
     """Each rank integrates its own draw of the workload (replicas, weak scaling)."""
     return seed + 1000 * rank
@@ -256,15 +297,29 @@ def run_reference(args, nbg, rank):
         "cpu_1core": {"value": v1, "unit": "system-steps/s", "cores": 1,
                       "sample": "%d systems of %s, %.1f s on one host thread" % (used1, args.workload, t1)},
     }
+    if args.secondary != "none":
+        sec = {}
+        for name in [w for w in args.secondary.split(",") if w and w != "serve"]:
+            v2, per_n, cores2, t2 = cpu_rate_by_n(nbg, name, args.seed)
+            sec[name] = {"value": v2, "unit": "system-steps/s", "cores": cores2, "kind": "port",
+                         "per_body_count": per_n,
+                         "sample": "per body count, systems of %s integrated for their first 1500 steps, one per "
+                                   "host thread, %.1f s in all; combined as the time of the whole workload" %
+                                   (name, t2)}
+        line["secondary"] = sec
     print(json.dumps(line), flush=True)
 
 
-def serve_stream(nbg, srv, pool, rate, nreq, seed, timeout_s):
+def serve_stream(nbg, srv, pool, rate, nreq, seed, timeout_s, fixed_tail=0):
     """Poisson arrivals (rate requests/s) of nreq requests drawn from pool;
-    returns (infos, wall seconds from first arrival to last completion)."""
+    returns (infos, wall seconds from first arrival to last completion).
+    The last fixed_tail entries of pool are sent once each, at random places
+    in the stream (their infos carry probe = True); the rest are drawn."""
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate, nreq) if rate > 0 else np.zeros(nreq)
-    picks = rng.integers(0, len(pool), nreq)
+    nbase = len(pool) - fixed_tail
+    picks = np.concatenate([rng.integers(0, nbase, nreq - fixed_tail), np.arange(nbase, len(pool))])
+    rng.shuffle(picks)
     ids, infos, lock = {}, [], threading.Lock()
     done = threading.Event()
     t_start = time.perf_counter()
@@ -281,7 +336,7 @@ def serve_stream(nbg, srv, pool, rate, nreq, seed, timeout_s):
             tt = nbg.TransitTiming(tmax, ic)
             rid = srv.submit(s, tt, nbg.Integrator(nbg.ahl21, h, 0.0, tmax), grad)
             with lock:
-                ids[rid] = (s, tt)
+                ids[rid] = (s, tt, picks[q] >= nbase)
 
     def collector():
         got = 0
@@ -296,7 +351,7 @@ def serve_stream(nbg, srv, pool, rate, nreq, seed, timeout_s):
                 if st is not None:
                     break
                 time.sleep(1e-4)  # the client has not recorded this id yet
-            infos.append(srv.result(rid, st[0], st[1]))
+            infos.append(dict(srv.result(rid, st[0], st[1]), probe=bool(st[2])))
             got += 1
         done.set()
 
@@ -343,6 +398,106 @@ def run_serve(args, nbg):
     return out
 
 
+def measure_secondary(nbg, workload, device, seed, tune_steps):
+    """One timed pass of a batch workload after the autotuner's trial runs (which warm its kernels
+    up): system-steps/s, the consumer's roofline and the clocks of the pass."""
+    import torch
+    ctx = nbg.Context(device)
+    states, timings, hs, tms, nsteps = build_workload(nbg, workload, None, seed)
+    b = make_batch(nbg, states, timings, hs, tms)
+    dev0 = {k: torch.from_numpy(a.copy()).cuda() for k, a in b.arrays.items()}
+    dev = {k: torch.empty_like(t) for k, t in dev0.items()}
+
+    def reset():
+        for k in dev:
+            dev[k].copy_(dev0[k])
+
+    reset()
+    t_tune = time.perf_counter()
+    tuning = b.autotune_device(dev, ctx, trial_steps=tune_steps)
+    t_tune = time.perf_counter() - t_tune
+    reset()
+    torch.cuda.synchronize()
+    clk = ClockSampler(device)
+    clk.start()
+    ctx.set_profiling(3)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    b.run_device(dev, ctx)
+    e1.record()
+    torch.cuda.synchronize()
+    ctx.set_profiling(0)
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1)
+    _, _, _, jac_ms = ctx.last_timing()
+    flops = sum(flops_per_system_step(s.n) * ns for s, ns in zip(states, nsteps))
+    peak = ctx.fp64_peak_tflops()
+    achieved = flops / (jac_ms * 1e-3) / 1e12 if jac_ms > 0 else None
+    total = int(sum(nsteps))
+    out = {"workload": workload, "nsys": len(states), "system_steps_per_pass": total,
+           "body_counts": sorted({int(s.n) for s in states}), "longest_system_steps": int(max(nsteps)),
+           "value": total / (ms * 1e-3), "unit": "system-steps/s", "ms_per_pass": ms, "timed_passes": 1,
+           "warmup": "the autotuner's trial runs (%.1f s)" % t_tune,
+           "launches": int(ctx.last_launch_count()),
+           "autotuner": {k: tuning[0][k] for k in ("chunk_steps", "orbit_team", "producer_warps", "producer_smem_kb")},
+           "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                        "frac": (achieved / peak) if achieved else None, "kernel": "jacobian_chunk_kernel",
+                        "kernel_ms": jac_ms, "peak_source": "measured live (nbg_fp64_peak, DFMA)"},
+           "clocks": clocks}
+    ctx.close()
+    del dev, dev0
+    torch.cuda.empty_cache()
+    return out
+
+
+def measure_serving(nbg, args, capacity):
+    """The request server on config-4 draws (batch_uneven systems, tmax log-uniform 100..4000 d, half with
+    gradient) arriving as a Poisson stream at 80 % of the GPU's capacity on this mix -- the batched
+    throughput `capacity` (system-steps/s) of batch_uneven, converted to requests/s by the pool's mean
+    request length -- with 8-body 1600-day gradient requests mixed in; p50 / p99 latency overall, per body
+    count and for the 8-body 1600-day class."""
+    W = nbg.workloads
+    els, hs, tms = W.batch_uneven(args.serve_pool, args.seed + 11)
+    rng = np.random.default_rng(args.seed + 12)
+    pool = []
+    for el, h, tmax in zip(els, hs, tms):
+        ic = W.ic_of(el)
+        pool.append((nbg.State(ic), ic, h, tmax, bool(rng.integers(0, 2))))
+    mean_steps = float(np.mean([abs(round(t / h)) for _, _, h, t, _ in pool]))
+    # the latency class of the target: 8-body systems drawn as batch_uneven, 1600 days, with gradient
+    e8, h8, _ = W.batch_uneven(args.serve_probe, args.seed + 13, nmin=8, nmax=8)
+    probes = [(nbg.State(W.ic_of(el)), W.ic_of(el), h, 1600.0, True) for el, h in zip(e8, h8)]
+    rate = 0.8 * capacity / mean_steps
+    nreq = args.serve_point_requests + len(probes)
+    with nbg.Server(slots_per_group=args.serve_slots, chunk_steps=args.serve_chunk) as srv:
+        infos, wall = serve_stream(nbg, srv, pool + probes, rate, nreq, args.seed + 101, args.serve_timeout,
+                                   fixed_tail=len(probes))
+        st = srv.stats()
+    ok = [i for i in infos if i["rc"] == 0]
+    lat = np.array([i["latency_ms"] for i in ok]) if ok else np.zeros(1)
+    per_n = {}
+    for nb in sorted({i["n"] for i in ok}):
+        l = np.array([i["latency_ms"] for i in ok if i["n"] == nb])
+        per_n[str(nb)] = {"requests": int(len(l)), "p50_ms": float(np.percentile(l, 50)),
+                          "p99_ms": float(np.percentile(l, 99))}
+    pr = np.array([i["latency_ms"] for i in ok if i.get("probe")])
+    run = np.array([i["run_ms"] for i in ok if i.get("probe")])
+    return {"workload": "serve_uneven", "requests": nreq, "completed": len(ok), "grad_fraction": 0.5,
+            "tmax_days": "log-uniform 100..4000 (uncapped)",
+            "load": {"rate_per_s": rate, "fraction_of_capacity": 0.8,
+                     "capacity": "batch_uneven batched throughput, %.0f system-steps/s; mean request %.0f steps"
+                                 % (capacity, mean_steps),
+                     "wall_s": wall, "system_steps_per_s": sum(i["nsteps"] for i in ok) / wall,
+                     "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                     "per_n": per_n, "chunks": st["chunks"], "kernels": st["kernels"], "groups": st["groups"]},
+            "class_8body_1600d": {"requests": int(len(pr)), "steps_each": [int(abs(round(1600.0 / h))) for h in h8],
+                                  "p50_ms": float(np.percentile(pr, 50)) if len(pr) else None,
+                                  "p99_ms": float(np.percentile(pr, 99)) if len(pr) else None,
+                                  "run_p50_ms": float(np.percentile(run, 50)) if len(run) else None,
+                                  "target_p99_ms": 50.0}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -378,6 +533,15 @@ def main():
     ap.add_argument("--serve-chunk", type=int, default=32)
     ap.add_argument("--serve-tmax-max", type=float, default=0.0, help="cap on a request's tmax (0: none)")
     ap.add_argument("--serve-timeout", type=float, default=600.0)
+    ap.add_argument("--secondary", default="batch_8body,batch_uneven,serve",
+                    help="after the headline: one timed pass of each listed batch workload and the serving point "
+                         "('none' to skip); single-GPU runs only")
+    ap.add_argument("--serve-point-requests", type=int, default=64,
+                    help="config-4 requests of the serving point (besides its 8-body 1600-day requests)")
+    ap.add_argument("--serve-capacity", type=float, default=2.5e5,
+                    help="system-steps/s taken as the GPU's capacity when batch_uneven is not measured first")
+    ap.add_argument("--serve-probe", type=int, default=6,
+                    help="8-body 1600-day gradient requests mixed into the serving point's load stream")
     ap.add_argument("--fp64-probe", action="store_true",
                     help="print the measured FP64 rates (DFMA; DMMA alone; DMMA interleaved with DFMA), then exit")
     args = ap.parse_args()
@@ -569,6 +733,17 @@ def main():
             line["cpu_baseline"] = {"value": v, "unit": "system-steps/s", "cores": cores, "kind": "port",
                                     "sample": "%d systems of %s, %.1f s on %s host threads" %
                                               (used, args.workload, t, cores)}
+        if world == 1 and args.secondary != "none":
+            del dev, dev0
+            torch.cuda.empty_cache()
+            sec = {}
+            for name in [w for w in args.secondary.split(",") if w]:
+                if name == "serve":
+                    cap = sec.get("batch_uneven", {}).get("value") or args.serve_capacity
+                    sec[name] = measure_serving(nbg, args, cap)
+                else:
+                    sec[name] = measure_secondary(nbg, name, local_rank, args.seed, args.tune_steps)
+            line["secondary"] = sec
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
