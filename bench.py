@@ -440,7 +440,9 @@ def measure_secondary(nbg, workload, device, seed, tune_steps):
            "value": total / (ms * 1e-3), "unit": "system-steps/s", "ms_per_pass": ms, "timed_passes": 1,
            "warmup": "the autotuner's trial runs (%.1f s)" % t_tune,
            "launches": int(ctx.last_launch_count()),
-           "autotuner": {k: tuning[0][k] for k in ("chunk_steps", "orbit_team", "producer_warps", "producer_smem_kb")},
+           "autotuner": dict({k: tuning[0][k] for k in ("chunk_steps", "orbit_team", "producer_warps",
+                                                          "producer_smem_kb")},
+                             predicted_ms=tuning[0]["ms"], predicted_over_measured=tuning[0]["ms"] / ms),
            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                         "frac": (achieved / peak) if achieved else None, "kernel": "jacobian_chunk_kernel",
                         "kernel_ms": jac_ms, "peak_source": "measured live (nbg_fp64_peak, DFMA)"},
@@ -571,9 +573,10 @@ def main():
         dfma = ctx.fp64_peak_tflops()
         mma, _ = ctx.fp64_mma_peak_tflops(False)
         mixed, share = ctx.fp64_mma_peak_tflops(True)
+        issue = {"%dw_%dc" % (w, c): ctx.fp64_warp_issue_cycles(w, c) for w in (1, 2, 4, 8) for c in (1, 8)}
         print(json.dumps({"fp64_probe": {"dfma_tflops": dfma, "dmma_tflops": mma, "dmma_plus_dfma_tflops": mixed,
-                                         "dfma_share_of_mixed": share, "unit": "TFLOP/s (FMA = 2 flops)"}}),
-              flush=True)
+                                         "dfma_share_of_mixed": share, "unit": "TFLOP/s (FMA = 2 flops)",
+                                         "cycles_per_warp_dfma_one_block": issue}}), flush=True)
         return
     ctx = nbg.Context(local_rank)
     if args.chunk or args.serial:

@@ -433,9 +433,13 @@ int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double
  * {64, 128} x orbit producer form {one lane per system, team of lanes} x
  * producer block layout {one warp; four warps holding 200 KB of shared
  * memory, operator and search blocks 32 KB} (nbg_set_producer_layout).  The
- * two trial times extrapolate
- * the chunk loop's time to the batch's longest system (pipeline fill and
- * drain plus a steady cost per step); the fastest candidate is kept on the
+ * two trial times give the loop's fill and drain and its time per step with
+ * the whole batch active.  For a batch of uneven length (its shortest system
+ * under half its longest) two more trials run only its longest systems (at
+ * most 32) for the chain's time per step, and the predicted time sums, step
+ * by step, the larger of the whole-batch cost scaled by the work still
+ * active and the chain cost; for an even batch it extrapolates the two
+ * trials to the longest system.  The fastest candidate is kept on the
  * context (as nbg_set_tuning / nbg_set_orbit_team / nbg_set_orbit_lanes
  * would).  Arrays as for nbg_batch_integrate_transits_device.  report (may
  * be NULL) receives up to report_len candidates; *nreport (may be NULL)
@@ -510,6 +514,13 @@ int nbg_fp64_peak(nbg_context* ctx, double* tflops);
  * tensor path adds FP64 throughput beside the FMA pipe.  No counterpart in
  * the reference; a measurement helper. */
 int nbg_fp64_mma_peak(nbg_context* ctx, int with_dfma, double* tflops, double* dfma_share);
+
+/* FP64 issue interval of one warp: `warps` warps (1..32) of a single block,
+ * each running `chains` (1, 2, 4 or 8) independent DFMA chains, timed with
+ * clock64; *cycles_per_dfma is the slowest warp's SM cycles per warp-DFMA.
+ * Shows the per-warp issue limit that bounds a one-system step's latency.
+ * No counterpart in the reference; a measurement helper. */
+int nbg_fp64_warp_issue(nbg_context* ctx, int warps, int chains, double* cycles_per_dfma);
 
 #ifdef __cplusplus
 }

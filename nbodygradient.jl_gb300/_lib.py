@@ -30,7 +30,7 @@ MAX_BODIES = 10
 EXPORTS = (
     "nbg_create", "nbg_destroy", "nbg_last_error", "nbg_version", "nbg_device_info",
     "nbg_integrate_transits", "nbg_batch_integrate_transits", "nbg_batch_integrate_transits_device",
-    "nbg_set_tuning", "nbg_last_timing", "nbg_last_launch_count", "nbg_fp64_peak", "nbg_fp64_mma_peak",
+    "nbg_set_tuning", "nbg_last_timing", "nbg_last_launch_count", "nbg_fp64_peak", "nbg_fp64_mma_peak", "nbg_fp64_warp_issue",
     "nbg_set_profiling", "nbg_last_kernel_stats", "nbg_set_orbit_lanes", "nbg_set_orbit_team",
     "nbg_set_producer_layout", "nbg_last_host_time",
     "nbg_batch_integrate_transits_noalloc",
@@ -142,6 +142,7 @@ def load(build_if_missing=True):
     L.nbg_last_launch_count.restype = ctypes.c_int64
     L.nbg_fp64_peak.argtypes = [_VP, _D]
     L.nbg_fp64_mma_peak.argtypes = [_VP, ctypes.c_int, _D, _D]
+    L.nbg_fp64_warp_issue.argtypes = [_VP, ctypes.c_int, ctypes.c_int, _D]
     L.nbg_set_profiling.argtypes = [_VP, ctypes.c_int]
     L.nbg_set_orbit_lanes.argtypes = [_VP, ctypes.c_int]
     L.nbg_set_orbit_team.argtypes = [_VP, ctypes.c_int]
@@ -265,6 +266,12 @@ class Context:
     def fp64_peak_tflops(self):
         v = ctypes.c_double()
         check(load().nbg_fp64_peak(self._h, ctypes.byref(v)))
+        return v.value
+
+    def fp64_warp_issue_cycles(self, warps, chains):
+        """SM cycles per warp-DFMA of the slowest of `warps` warps of one block running `chains` chains."""
+        v = ctypes.c_double()
+        check(load().nbg_fp64_warp_issue(self._h, int(warps), int(chains), ctypes.byref(v)))
         return v.value
 
     def fp64_mma_peak_tflops(self, with_dfma=False):

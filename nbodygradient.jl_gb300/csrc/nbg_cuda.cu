@@ -1130,6 +1130,30 @@ __global__ void fp64_peak_kernel(double* out, int iters) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// Single-block FP64 issue probe: `warps` warps of one block run CH
+// independent DFMA chains each and time them with clock64; cyc[w] is warp
+// w's cycle count.  One block, so every warp shares one SM.  out holds
+// blockDim doubles, cyc one entry per warp.
+template <int CH>
+__global__ void fp64_issue_kernel(double* out, long long* cyc, int iters) {
+  double a[CH];
+  const double b = 1.0000001 + 1e-9 * threadIdx.x, c = 1e-7;
+#pragma unroll
+  for (int k = 0; k < CH; k++) a[k] = 1.0 + k * 1e-3;
+  __syncthreads();
+  const long long t0 = clock64();
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int k = 0; k < CH; k++) a[k] = fma(a[k], b, c);
+  }
+  const long long t1 = clock64();
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < CH; k++) s += a[k];
+  out[threadIdx.x] = s;
+  if ((threadIdx.x & 31) == 0) cyc[threadIdx.x >> 5] = t1 - t0;
+}
+
 // FP64 tensor-core (DMMA) probes: mma.sync m8n8k4 with f64 operands, one
 // 8x4 by 4x8 product into an 8x8 accumulator per warp instruction (256 FMAs).
 // Fragments (PTX ISA, mma.m8n8k4 .f64): lane l holds A[l/4][l%4],
@@ -1351,6 +1375,37 @@ int nbg_fp64_peak(nbg_context* ctx, double* tflops) {
     best = std::min(best, ms);
   }
   *tflops = 2.0 * (double)blocks * threads * iters * PEAK_CHAINS / (best * 1e-3) / 1e12;
+  return NBG_OK;
+}
+
+int nbg_fp64_warp_issue(nbg_context* ctx, int warps, int chains, double* cycles_per_dfma) {
+  if (!ctx || !cycles_per_dfma) return set_error(NBG_EINVAL, "NULL argument");
+  if (warps < 1 || warps > 32) return set_error(NBG_EINVAL, "warps = %d not in 1..32", warps);
+  if (chains != 1 && chains != 2 && chains != 4 && chains != 8)
+    return set_error(NBG_EINVAL, "chains = %d not 1, 2, 4 or 8", chains);
+  NBG_CUDA(cudaSetDevice(ctx->device));
+  double* out;
+  long long* cyc;
+  int rc;
+  if ((rc = ctx->get("issue_out", (size_t)32 * warps, &out))) return rc;
+  if ((rc = ctx->get("issue_cyc", (size_t)warps, &cyc))) return rc;
+  const int iters = 2000;
+  for (int pass = 0; pass < 2; pass++) {  // the first pass warms the instruction cache
+    const int it = pass ? iters : 10;
+    switch (chains) {
+      case 1: fp64_issue_kernel<1><<<1, 32 * warps, 0, ctx->stream>>>(out, cyc, it); break;
+      case 2: fp64_issue_kernel<2><<<1, 32 * warps, 0, ctx->stream>>>(out, cyc, it); break;
+      case 4: fp64_issue_kernel<4><<<1, 32 * warps, 0, ctx->stream>>>(out, cyc, it); break;
+      default: fp64_issue_kernel<8><<<1, 32 * warps, 0, ctx->stream>>>(out, cyc, it); break;
+    }
+    NBG_CUDA(cudaGetLastError());
+  }
+  long long h[32];
+  NBG_CUDA(cudaMemcpyAsync(h, cyc, sizeof(long long) * warps, cudaMemcpyDeviceToHost, ctx->stream));
+  NBG_CUDA(cudaStreamSynchronize(ctx->stream));
+  long long mx = 0;
+  for (int w = 0; w < warps; w++) mx = std::max(mx, h[w]);
+  *cycles_per_dfma = (double)mx / ((double)iters * chains);
   return NBG_OK;
 }
 
@@ -1750,10 +1805,16 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
   if (trial_steps < 8 || trial_steps > 100000) return set_error(NBG_EINVAL, "trial_steps = %d", trial_steps);
   NBG_CUDA(cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
-  // two trials per candidate: every system's first min(nsteps, T) steps for
-  // T = trial_steps and 2 trial_steps, on copies.  The loop time is close to
-  // affine in T (pipeline fill and drain, then a steady cost per step), so the
-  // two trials extrapolate it to the batch's longest system.
+  // Trials per candidate, on copies: every system's first min(nsteps, T)
+  // steps for T = trial_steps and 2 trial_steps give the loop's fill and
+  // drain and its time per step with the whole batch active (close to affine
+  // in T).  A batch of uneven length is not all active to its end: once its
+  // short systems have finished, a step costs what its longest systems'
+  // chains cost.  For such a batch two more trials run the longest systems
+  // alone (T and 2T steps) for the chain's time per step, and the loop time
+  // is modelled step by step as the larger of the whole-batch cost scaled by
+  // the work still active (systems weighted by their Jacobian work per step)
+  // and the chain cost.
   std::vector<nbg_system_desc> td1(desc, desc + nsys), td2(desc, desc + nsys);
   long long ax = 0, am = 0, aJ = 0, adq = 0, ap = 0, att = 0, adq0 = 0, steps = 0, longest = 0;
   bool any_team = false;
@@ -1773,6 +1834,33 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
     att += (long long)n * desc[s].ntt; adq0 += (long long)n * desc[s].ntt * 7 * n;
   }
   if (steps == 0) return set_error(NBG_EINVAL, "the batch has no steps to time");
+  // the step distribution: (steps, weight) sorted by steps, and the chain set
+  std::vector<std::pair<long long, double>> dist(nsys);
+  long long shortest = longest;
+  double wtot = 0.0;
+  for (int s = 0; s < nsys; s++) {
+    const int n = desc[s].n, P = n * (n - 1) / 2;
+    const double w = 7.0 * n * (264.0 * P + 18.0 * n * n + 87.0 * n);  // consumer flops per system-step
+    dist[s] = {steps_of(desc[s].h, desc[s].tmax), w};
+    shortest = std::min(shortest, dist[s].first);
+    wtot += w;
+  }
+  std::sort(dist.begin(), dist.end());
+  const bool uneven = longest > 0 && (double)shortest < 0.5 * (double)longest;
+  // the chain set: the longest systems (at most 32), the rest shortened to zero steps
+  std::vector<nbg_system_desc> tc1(td1), tc2(td2);
+  if (uneven) {
+    std::vector<int> ord(nsys);
+    for (int s = 0; s < nsys; s++) ord[s] = s;
+    std::sort(ord.begin(), ord.end(), [&](int a, int b) {
+      return steps_of(desc[a].h, desc[a].tmax) > steps_of(desc[b].h, desc[b].tmax);
+    });
+    const int nchain = std::min(32, std::max(1, nsys / 64));
+    for (int q = nchain; q < nsys; q++) {
+      tc1[ord[q]].tmax = 0.0;
+      tc2[ord[q]].tmax = 0.0;
+    }
+  }
   std::vector<double> th(nsys);
   std::vector<uint8_t> ph(ap);
   NBG_CUDA(cudaMemcpy(th.data(), t, sizeof(double) * nsys, cudaMemcpyDeviceToHost));
@@ -1826,18 +1914,35 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
     ctx->prod_warps = cd.pw;
     ctx->prod_smem_kb = cd.smem;
     ctx->guard_smem_kb = cd.guard;
-    double tms[2] = {0.0, 0.0};
-    for (int r = 0; r < 2 && !rc; r++) {
+    double tms[4] = {0.0, 0.0, 0.0, 0.0};
+    const int ntrials = (uneven && q > 0) ? 4 : 2;
+    for (int r = 0; r < ntrials && !rc; r++) {
       if ((rc = reset())) break;
-      rc = run_batch(ctx, nsys, r ? td2.data() : td1.data(), th.data(), ph.data(), c_t, c_x, c_v, m, c_xe, c_ve, c_J,
-                     c_E, c_dq, jac_init, c_tt, c_dq0, c_del, c_cnt, nullptr);
+      const nbg_system_desc* dd = r == 0 ? td1.data() : r == 1 ? td2.data() : r == 2 ? tc1.data() : tc2.data();
+      rc = run_batch(ctx, nsys, dd, th.data(), ph.data(), c_t, c_x, c_v, m, c_xe, c_ve, c_J, c_E, c_dq, jac_init, c_tt,
+                     c_dq0, c_del, c_cnt, nullptr);
       tms[r] = ctx->last_total_ms;
     }
     if (rc) break;
     if (q == 0) continue;
     const double T1 = std::min<long long>(longest, trial_steps), T2 = std::min<long long>(longest, 2LL * trial_steps);
-    const double slope = (T2 > T1) ? (tms[1] - tms[0]) / (T2 - T1) : 0.0;
-    const double ms = (T2 > T1) ? tms[0] + std::max(0.0, slope) * ((double)longest - T1) : tms[1];
+    const double slope = (T2 > T1) ? std::max(0.0, (tms[1] - tms[0]) / (T2 - T1)) : 0.0;
+    double ms = (T2 > T1) ? tms[0] + slope * ((double)longest - T1) : tms[1];
+    if (uneven && T2 > T1) {
+      const double fill = std::max(0.0, tms[0] - slope * T1);
+      const double chain = std::max(0.0, (tms[3] - tms[2]) / (T2 - T1));
+      // walk the steps: between consecutive system lengths the active work is constant
+      double model = fill, active = wtot;
+      long long k = 0;
+      size_t at = 0;
+      while (at < dist.size() && k < longest) {
+        while (at < dist.size() && dist[at].first <= k) active -= dist[at++].second;
+        const long long next = at < dist.size() ? dist[at].first : longest;
+        model += (double)(next - k) * std::max(slope * active / wtot, chain);
+        k = next;
+      }
+      ms = model;
+    }
     if (report && nrep < report_len) {
       memset(&report[nrep], 0, sizeof(report[nrep]));
       report[nrep].chunk_steps = cd.chunk;

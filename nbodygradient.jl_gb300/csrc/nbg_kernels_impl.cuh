@@ -134,12 +134,91 @@ __global__ void __launch_bounds__(PROD_BS * PROD_MAX_WARPS) orbit_chunk_kernel(G
 // from the end-of-step state, then (grad) the partial step at the converged
 // dt0 with its operator records and the adjoint row u^T = w^T S(dt0) that the
 // Jacobian consumer turns into dtdq0 (dtbvdq! row 1, timing.jl:155-171).
-// One lane per search, grid-stride over the queue.
 // The iterations take x, v only and the physical time derivative of g
 // (gdot_physical) where the reference builds the full gradient step to read
 // g's step derivative: both iterations stop at the same root of g to
 // rounding; the converged search's step keeps the reference's derivative,
 // which dtdq0 divides by.
+//
+// Everything after the Newton iterations, for one search on one lane: st is
+// the search's start state, wk the last iterate's state, dt0 the converged
+// step; the operator records of the final partial step go to this lane's
+// column `lane_id` of tscratch (lane_ids in 0..lanes-1).
+template <int N>
+__device__ void search_finish(const GroupArgs& g, int s, int slot, int c, int ib, int ti, const Sys<N>& st,
+                              Sys<N>& wk, double dt0, double t, int iter, Work<N>& w, int lane_id, int lanes) {
+  const int S = g.S;
+  const uint64_t kick = g.kick;
+  if (iter >= 20) atomicOr(g.status + s, NBG_STATUS_NEWTON_ITMAX);
+  const int nr = g.tbv ? 3 : 1;
+  double* ttout = g.tt + g.off_tt[g.sysidx[s]] + (long long)nr * (ib + (long long)N * c);
+  if (g.tbv && !g.grad) {
+    // TransitParameters without gradient (timing.jl:96-97): v_sky and
+    // b_sky^2 of the last Newton iteration's state
+    const double dvx = wk.v[3 * ib] - wk.v[3 * ti], dvy = wk.v[3 * ib + 1] - wk.v[3 * ti + 1];
+    const double dx = wk.x[3 * ib] - wk.x[3 * ti], dy = wk.x[3 * ib + 1] - wk.x[3 * ti + 1];
+    ttout[1] = sqrt(dvx * dvx + dvy * dvy);
+    ttout[2] = dx * dx + dy * dy;
+  }
+  if (g.grad) {
+    wk = st;
+    Rec rec{g.tscratch + lane_id, lanes};
+    ahl21_step<N, true, true>(wk, w, dt0, kick, rec, Rec{nullptr, 0}, Rec{nullptr, 0});
+    double u[7 * N];
+    for (int q = 0; q < 7 * N; q++) u[q] = 0.0;
+    const double dvx = wk.v[3 * ib] - wk.v[3 * ti], dvy = wk.v[3 * ib + 1] - wk.v[3 * ti + 1];
+    const double dx = wk.x[3 * ib] - wk.x[3 * ti], dy = wk.x[3 * ib + 1] - wk.x[3 * ti + 1];
+    u[7 * ib + 0] = dvx;
+    u[7 * ti + 0] = -dvx;
+    u[7 * ib + 1] = dvy;
+    u[7 * ti + 1] = -dvy;
+    u[7 * ib + 3] = dx;
+    u[7 * ti + 3] = -dx;
+    u[7 * ib + 4] = dy;
+    u[7 * ti + 4] = -dy;
+    adjoint_step<N>(u, dt0, kick, rec);
+    const double gd = gdot(wk, ti, ib);
+    double* tr = g.trec + ((size_t)slot * trec_size(N, g.tbv)) * S + s;
+    for (int q = 0; q < 7 * N; q++) tr[(size_t)q * S] = u[q];
+    if (g.tbv) {
+      // dtbvdq! rows 2 and 3 (timing.jl:173-191): v_sky and b_sky^2 of the
+      // converged state, dv_sky/dt, and the adjoint rows of their
+      // numerators (d v_sky: the sky velocity difference on the velocity
+      // rows; d b_sky^2 / 2: the sky position difference on the position rows)
+      const double vsky = sqrt(dvx * dvx + dvy * dvy);
+      const double bsky2 = dx * dx + dy * dy;
+      const double* q = wk.dqdt;
+      const double dvdt = (dvx * (q[7 * ib + 3] - q[7 * ti + 3]) + dvy * (q[7 * ib + 4] - q[7 * ti + 4])) / vsky;
+      for (int r = 0; r < 2; r++) {
+        for (int e = 0; e < 7 * N; e++) u[e] = 0.0;
+        if (r == 0) {
+          u[7 * ib + 3] = dvx;
+          u[7 * ti + 3] = -dvx;
+          u[7 * ib + 4] = dvy;
+          u[7 * ti + 4] = -dvy;
+        } else {
+          u[7 * ib + 0] = dx;
+          u[7 * ti + 0] = -dx;
+          u[7 * ib + 1] = dy;
+          u[7 * ti + 1] = -dy;
+        }
+        adjoint_step<N>(u, dt0, kick, rec);
+        for (int e = 0; e < 7 * N; e++) tr[(size_t)(7 * N * (r + 1) + e) * S] = u[e];
+      }
+      tr[(size_t)(21 * N) * S] = gd;
+      tr[(size_t)(21 * N + 1) * S] = vsky;
+      tr[(size_t)(21 * N + 2) * S] = dvdt;
+      ttout[1] = vsky;
+      ttout[2] = bsky2;
+    } else {
+      tr[(size_t)(7 * N) * S] = gd;
+    }
+    g.tflag[(size_t)slot * S + s] = c;
+  }
+  ttout[0] = t + dt0;
+}
+
+// One lane per search, grid-stride over the queue.
 template <int N>
 __global__ void __launch_bounds__(TRANSIT_BS) transit_kernel(GroupArgs g, int chunk) {
   const int ntask = min(*g.task_count, g.task_cap);
@@ -181,76 +260,107 @@ __global__ void __launch_bounds__(TRANSIT_BS) transit_kernel(GroupArgs g, int ch
       iter += 1;
       if (iter >= 20 || dt0 == tt1 || dt0 == tt2) break;
     }
-    if (iter >= 20) atomicOr(g.status + s, NBG_STATUS_NEWTON_ITMAX);
-    const int nr = g.tbv ? 3 : 1;
-    double* ttout = g.tt + g.off_tt[g.sysidx[s]] + (long long)nr * (ib + (long long)N * c);
-    if (g.tbv && !g.grad) {
-      // TransitParameters without gradient (timing.jl:96-97): v_sky and
-      // b_sky^2 of the last Newton iteration's state
-      const double dvx = wk.v[3 * ib] - wk.v[3 * ti], dvy = wk.v[3 * ib + 1] - wk.v[3 * ti + 1];
-      const double dx = wk.x[3 * ib] - wk.x[3 * ti], dy = wk.x[3 * ib + 1] - wk.x[3 * ti + 1];
-      ttout[1] = sqrt(dvx * dvx + dvy * dvy);
-      ttout[2] = dx * dx + dy * dy;
-    }
-    if (g.grad) {
-      wk = st;
-      Rec rec{g.tscratch + tid, G};
-      ahl21_step<N, true, true>(wk, w, dt0, kick, rec, Rec{nullptr, 0}, Rec{nullptr, 0});
-      double u[7 * N];
-      for (int q = 0; q < 7 * N; q++) u[q] = 0.0;
-      const double dvx = wk.v[3 * ib] - wk.v[3 * ti], dvy = wk.v[3 * ib + 1] - wk.v[3 * ti + 1];
-      const double dx = wk.x[3 * ib] - wk.x[3 * ti], dy = wk.x[3 * ib + 1] - wk.x[3 * ti + 1];
-      u[7 * ib + 0] = dvx;
-      u[7 * ti + 0] = -dvx;
-      u[7 * ib + 1] = dvy;
-      u[7 * ti + 1] = -dvy;
-      u[7 * ib + 3] = dx;
-      u[7 * ti + 3] = -dx;
-      u[7 * ib + 4] = dy;
-      u[7 * ti + 4] = -dy;
-      adjoint_step<N>(u, dt0, kick, rec);
-      const double gd = gdot(wk, ti, ib);
-      double* tr = g.trec + ((size_t)slot * trec_size(N, g.tbv)) * S + s;
-      for (int q = 0; q < 7 * N; q++) tr[(size_t)q * S] = u[q];
-      if (g.tbv) {
-        // dtbvdq! rows 2 and 3 (timing.jl:173-191): v_sky and b_sky^2 of the
-        // converged state, dv_sky/dt, and the adjoint rows of their
-        // numerators (d v_sky: the sky velocity difference on the velocity
-        // rows; d b_sky^2 / 2: the sky position difference on the position rows)
-        const double vsky = sqrt(dvx * dvx + dvy * dvy);
-        const double bsky2 = dx * dx + dy * dy;
-        const double* q = wk.dqdt;
-        const double dvdt = (dvx * (q[7 * ib + 3] - q[7 * ti + 3]) + dvy * (q[7 * ib + 4] - q[7 * ti + 4])) / vsky;
-        for (int r = 0; r < 2; r++) {
-          for (int e = 0; e < 7 * N; e++) u[e] = 0.0;
-          if (r == 0) {
-            u[7 * ib + 3] = dvx;
-            u[7 * ti + 3] = -dvx;
-            u[7 * ib + 4] = dvy;
-            u[7 * ti + 4] = -dvy;
-          } else {
-            u[7 * ib + 0] = dx;
-            u[7 * ti + 0] = -dx;
-            u[7 * ib + 1] = dy;
-            u[7 * ti + 1] = -dy;
-          }
-          adjoint_step<N>(u, dt0, kick, rec);
-          for (int e = 0; e < 7 * N; e++) tr[(size_t)(7 * N * (r + 1) + e) * S] = u[e];
-        }
-        tr[(size_t)(21 * N) * S] = gd;
-        tr[(size_t)(21 * N + 1) * S] = vsky;
-        tr[(size_t)(21 * N + 2) * S] = dvdt;
-        ttout[1] = vsky;
-        ttout[2] = bsky2;
-      } else {
-        tr[(size_t)(7 * N) * S] = gd;
-      }
-      g.tflag[(size_t)slot * S + s] = c;
-    }
-    ttout[0] = t + dt0;
+    search_finish<N>(g, s, slot, c, ib, ti, st, wk, dt0, t, iter, w, tid, G);
   }
 }
 
+// Shared memory of the team search per warp: per team the search's start
+// state, the Newton iterate and the accelerations of phisalpha!.
+template <int N>
+__host__ __device__ constexpr int search_team_smem_bytes() {
+  return (PROD_BS / team_lanes(N)) * (int)(2 * sizeof(Sys<N>) + 3 * N * sizeof(double));
+}
+
+// Team form of the searches (groups without kick pairs): a team of
+// L = team_lanes(N) lanes per search, T = 32 / L searches per warp, one warp
+// per block.  The Newton iterations run the level-parallel step of the team
+// producer (team_step, bitwise the one-lane no-gradient step) on the
+// team's shared-memory copy of the state, so their critical path is
+// 2(2N - 3) pair solves per iteration instead of N(N - 1); every lane of a
+// team computes g, its derivative and the update of dt0 from the same
+// shared values, so a team stops together.  The final partial step with its
+// records and the adjoint rows run on the team's first lane
+// (search_finish), as in the one-lane kernel.  Results are bitwise those of
+// transit_kernel.
+template <int N>
+__global__ void __launch_bounds__(TRANSIT_BS) transit_team_kernel(GroupArgs g, int chunk) {
+  constexpr int L = team_lanes(N);
+  constexpr int T = PROD_BS / L;
+  extern __shared__ double search_smem[];
+  Sys<N>* st0 = reinterpret_cast<Sys<N>*>(search_smem);
+  Sys<N>* wks = st0 + T;
+  double(*acc)[3 * N] = reinterpret_cast<double(*)[3 * N]>(wks + T);
+  const int ntask = min(*g.task_count, g.task_cap);
+  const int lane = threadIdx.x & 31;
+  const int team = lane / L, t = lane % L;
+  const bool in_team = team < T;
+  const int tm = in_team ? team : 0;  // idle lanes alias team 0 but never write
+  const int S = g.S;
+  const int teams = gridDim.x * T;
+  Work<N> w;
+  for (int base = blockIdx.x * T; base < ntask; base += teams) {
+    const int idx = base + tm;
+    const bool has = in_team && idx < ntask;
+    int s = 0, slot = 0, c = 0, ti = 0, ib = 0;
+    double dt0 = 0.0, t_end = 0.0;
+    if (has) {
+      const int* tk = g.task_i + 3 * idx;
+      s = tk[0];
+      slot = tk[1];
+      c = tk[2];
+      const int o = slot % (N - 1);
+      ti = g.ti[s];
+      ib = (o < ti) ? o : o + 1;
+      const double* tf = g.task_f + (size_t)idx * (12 * N + 2);
+      for (int q = t; q < 3 * N; q += L) {
+        st0[tm].x[q] = tf[q];
+        st0[tm].v[q] = tf[3 * N + q];
+        st0[tm].xe[q] = tf[6 * N + q];
+        st0[tm].ve[q] = tf[9 * N + q];
+      }
+      for (int q = t; q < N; q += L) st0[tm].m[q] = g.m[q * S + s];
+      for (int q = t; q < 7 * N; q += L) st0[tm].dqdt[q] = 0.0;
+      dt0 = tf[12 * N];
+      t_end = tf[12 * N + 1];
+    }
+    __syncwarp();
+    double stmp = 0.0, tt1 = dt0 + 1.0, tt2 = dt0 + 2.0;
+    int iter = 0;
+    bool active = has;
+    while (__any_sync(0xffffffffu, active)) {
+      if (active) {
+        tt2 = tt1;
+        tt1 = dt0;
+        for (int q = t; q < 3 * N; q += L) {
+          wks[tm].x[q] = st0[tm].x[q];
+          wks[tm].v[q] = st0[tm].v[q];
+          wks[tm].xe[q] = st0[tm].xe[q];
+          wks[tm].ve[q] = st0[tm].ve[q];
+        }
+        for (int q = t; q < N; q += L) wks[tm].m[q] = st0[tm].m[q];
+      }
+      __syncwarp();
+      team_step<N>(wks[tm], acc[tm], w, t, active, dt0, Rec{nullptr, 0}, Rec{nullptr, 0});
+      __syncwarp();
+      if (active) {
+        const double gs = gsky(wks[tm], ti, ib);
+        const double gd = gdot_physical(wks[tm], ti, ib);
+        const double dt = -gs / gd;
+        kahan(dt0, stmp, dt);
+        iter += 1;
+        if (iter >= 20 || dt0 == tt1 || dt0 == tt2) active = false;
+      }
+      __syncwarp();
+    }
+    if (has && t == 0) {
+      Sys<N> st = st0[tm];
+      Sys<N> wk = wks[tm];
+      search_finish<N>(g, s, slot, c, ib, ti, st, wk, dt0, t_end, iter, w,
+                       blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+    }
+    __syncwarp();
+  }
+}
 
 // Kepler-pair records of one chunk: one lane per (step, pair slot, system),
 // consecutive lanes = consecutive systems, so a warp shares its pair.
@@ -453,6 +563,12 @@ int launch_jac(const GroupArgs& g, int chunk, cudaStream_t st) {
 
 template <int N>
 int launch_transit(const GroupArgs& g, int chunk, cudaStream_t st) {
+  if (team_lanes(N) > 1 && g.team && !g.kick) {
+    const int smem = std::max(search_team_smem_bytes<N>(), g.guard_smem);
+    allow_smem(transit_team_kernel<N>, smem);
+    transit_team_kernel<N><<<g.tgrid / TRANSIT_BS, TRANSIT_BS, smem, st>>>(g, chunk);
+    return 0;
+  }
   allow_smem(transit_kernel<N>, g.guard_smem);
   transit_kernel<N><<<g.tgrid / TRANSIT_BS, TRANSIT_BS, g.guard_smem, st>>>(g, chunk);
   return 0;

@@ -13,18 +13,23 @@ the same span on host threads (concurrently with the GPU run):
 
 Gates.  batch_3body uses the tolerances of tests/parity.py: tt within 1e-10
 of the span, dtdq0 and dtdelements within 1e-8 relative entry by entry (with
-the floor of 1e-4 of the transit row's scale).  The two chaotic long spans
-(batch_8body over 26 667 steps, batch_uneven up to 77 k) keep the tt gate and
-identical counts and take the derivatives normwise per transit row: for each
-transit (body j, transit c), max |gpu - ref| <= 1e-8 max |ref| over its 7N
-entries -- the maxabs-norm isapprox of the reference's own test
-(test/test_transit_timing.jl:87-88, there over the whole array with
-rtol = sqrt(eps)), applied row by row.  Over these spans the entrywise rule is
-below what FP64 reproduces: the oracle built on x86-64 and on AArch64 (same
-source, different libm) disagrees with itself in 0.5-1 % of the 8-body
-entries by up to 400x the entrywise tolerance, as much as the GPU disagrees
-with it, and a one-ulp change of one initial coordinate moves 0.2-0.4 % of
-them by up to 150x.  The entrywise figures are still measured and reported.
+the floor of 1e-4 of the transit row's scale).
+
+The two long spans (batch_8body over 26 667 steps, batch_uneven up to 77 k)
+are chaotic enough that FP64 does not reproduce them to those tolerances:
+the oracle built on x86-64 and on AArch64 (same source, different libm)
+disagrees with itself as much as the GPU disagrees with it.  They keep the
+tt gate (1e-10 of the span) and identical counts, and measure everything
+else against the reference's own reproducibility, which the test measures:
+each sampled system is also run through the oracle with one initial
+coordinate moved by one ulp.  A transit row (body j, transit c) of dtdq0 or
+dtdelements passes when its largest deviation from the oracle, relative to
+the row's largest entry (the maxabs norm of the reference's own test,
+test/test_transit_timing.jl:87-88, applied per row), is within 1e-8, or
+within 10 times the relative deviation that the one-ulp change causes in the
+oracle's own rows up to that time.  x, v and each jac_step column follow the
+same rule (1e-10 for x and v, 1e-8 per column).  The entrywise figures are
+measured and reported.
 
 Each test writes its worst ratios (error / tolerance, 1.0 = at the bound) to
 the JSON-lines file named by NBG_PARITY_REPORT when that variable is set.
@@ -56,14 +61,21 @@ def _report(name, **vals):
             f.write(json.dumps(dict(test=name, **vals)) + "\n")
 
 
+ULP_FACTOR = 10.0
+
+
 def _oracle_runs(jobs):
-    """Runs (state, h, tmax, ntt) jobs through the oracle on host threads; returns a future of
-    [(OState, OTiming)].  ctypes releases the GIL, so the GPU run proceeds meanwhile."""
+    """Runs (state, h, tmax, ntt, perturbed) jobs through the oracle on host threads; returns a future
+    of [(OState, OTiming)].  A perturbed job moves the first planet's x coordinate up by one ulp.
+    ctypes releases the GIL, so the GPU run proceeds meanwhile."""
     threads = max(1, (os.cpu_count() or 2) - 2)
 
     def one(job):
-        s, h, tmax, ntt = job
-        so = O.OState(s.x, s.v, s.m, jac_init=s.jac_init)
+        s, h, tmax, ntt, pert = job
+        x = s.x.copy(order="F")
+        if pert:
+            x[0, 1] = np.nextafter(x[0, 1], np.inf)
+        so = O.OState(x, s.v, s.m, jac_init=s.jac_init)
         to = O.OTiming(s.n, ntt, 0)
         O.integrate_transits(so, to, h, tmax)
         return so, to
@@ -91,9 +103,35 @@ def _gpu_batch(states, hs, tms, ntts):
     return b
 
 
-def _compare_system(b, q, so, to, tmax, normwise):
+def _rows_within_reproducibility(gpu, ref, alt, tt, count, name):
+    """Per transit row: the relative deviation e of gpu from ref and the one-ulp oracle's relative
+    deviation d from ref, rows in time order; a row passes when e <= max(1e-8, ULP_FACTOR * (largest d
+    so far)).  Returns (worst e / 1e-8, rows passing only through the reproducibility bound)."""
+    rows = []
+    for j, c in enumerate(count):
+        for t in range(min(int(c), gpu.shape[1])):
+            s = float(np.max(np.abs(ref[j, t])))
+            if s == 0.0:
+                assert np.all(gpu[j, t] == 0.0), (name, j, t)
+                continue
+            rows.append((float(tt[j, t]), j, t, float(np.max(np.abs(gpu[j, t] - ref[j, t]))) / s,
+                         float(np.max(np.abs(alt[j, t] - ref[j, t]))) / s))
+    rows.sort()
+    env, worst, by_env = 0.0, 0.0, 0
+    for time, j, t, e, d in rows:
+        env = max(env, d)
+        worst = max(worst, e / P.DT_RTOL)
+        if e > P.DT_RTOL:
+            by_env += 1
+            assert e <= ULP_FACTOR * env, ("%s[%d,%d] at t = %.3f: deviation %.3g of the row scale, beyond 1e-8 and "
+                                           "beyond %g x the one-ulp spread so far (%.3g)" % (name, j, t, time, e,
+                                                                                             ULP_FACTOR, env))
+    return worst, by_env
+
+
+def _compare_system(b, q, so, to, tmax, normwise, alt=None):
     """Worst tolerance ratios of system q of the GPU batch against the oracle run (normwise: the
-    transit derivatives per transit row; else entry by entry)."""
+    transit derivatives per transit row, with alt = the one-ulp oracle run; else entry by entry)."""
     n = int(b.n[q])
     ntt = int(b.ntt[q])
     M = 7 * n
@@ -103,8 +141,11 @@ def _compare_system(b, q, so, to, tmax, normwise):
     g_de = b.view("dtdelements", q).reshape((n, ntt, 7, n), order="F")
     out = {"n": n, "transits": int(to.count.sum()), "tt": err_tt / (P.TT_TOL * abs(tmax))}
     if normwise:
-        out["dtdq0"] = P.check_rows_normwise(g_dq, to.dtdq0, to.count, "dtdq0")
-        out["dtdelements"] = P.check_rows_normwise(g_de, to.dtdelements, to.count, "dtdelements")
+        so_a, to_a = alt
+        out["dtdq0"], out["dtdq0_rows_by_ulp_bound"] = _rows_within_reproducibility(
+            g_dq, to.dtdq0, to_a.dtdq0, to.tt, to.count, "dtdq0")
+        out["dtdelements"], out["dtdelements_rows_by_ulp_bound"] = _rows_within_reproducibility(
+            g_de, to.dtdelements, to_a.dtdelements, to.tt, to.count, "dtdelements")
         a = _excess(g_dq, to.dtdq0, to.count)
         e = _excess(g_de, to.dtdelements, to.count, to.dtdq0, so.jac_init)
         out["entrywise"] = {"dtdq0_beyond": a[1], "dtdq0_checked": a[0], "dtdq0_worst": a[2],
@@ -122,9 +163,12 @@ def _compare_system(b, q, so, to, tmax, normwise):
         P.check_state(gs, so)
     else:
         st = _state_ratios(gs, so)
+        sp = _state_ratios(so_a, so)
         out["state"] = st
-        assert st["x"] <= 1e-10 and st["v"] <= 1e-10, st
-        assert st["jac_step_columns"] <= 1e-8, st
+        out["state_one_ulp"] = sp
+        assert st["x"] <= max(1e-10, ULP_FACTOR * sp["x"]), (st, sp)
+        assert st["v"] <= max(1e-10, ULP_FACTOR * sp["v"]), (st, sp)
+        assert st["jac_step_columns"] <= max(1e-8, ULP_FACTOR * sp["jac_step_columns"]), (st, sp)
     return out
 
 
@@ -188,7 +232,9 @@ def _dump(name, q, b, so, to):
 
 
 def _run_and_compare(name, states, hs, tms, ntts, sample, normwise=False):
-    jobs = [(states[q], hs[q], tms[q], ntts[q]) for q in sample]
+    jobs = [(states[q], hs[q], tms[q], ntts[q], False) for q in sample]
+    if normwise:
+        jobs += [(states[q], hs[q], tms[q], ntts[q], True) for q in sample]
     runs = _oracle_runs(jobs)
     b = _gpu_batch(states, hs, tms, ntts)
     b.run()
@@ -198,10 +244,11 @@ def _run_and_compare(name, states, hs, tms, ntts, sample, normwise=False):
     assert len(nonfinite) == 0, "non-finite systems: %s" % nonfinite.tolist()
     overflow = np.nonzero(b.status & nbg._lib.NBG_STATUS_NTT_OVERFLOW)[0].tolist()
     results = runs.result()
+    alts = results[len(sample):] if normwise else [None] * len(sample)
     rows, failures = [], []
-    for q, (so, to) in zip(sample, results):
+    for q, (so, to), alt in zip(sample, results[:len(sample)], alts):
         try:
-            r = _compare_system(b, q, so, to, tms[q], normwise)
+            r = _compare_system(b, q, so, to, tms[q], normwise, alt)
         except AssertionError as e:
             failures.append("system %d (n = %d, %d steps): %s [%s]" % (q, int(b.n[q]), abs(round(tms[q] / hs[q])), e,
                                                                         _failure_stats(b, q, so, to)))

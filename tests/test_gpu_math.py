@@ -112,3 +112,17 @@ def test_fp64_tensor_core_probe_runs_and_checks_its_fragments():
         ctx.close()
     assert mma > 0 and mixed > 0
     assert share0 == 0.0 and 0.0 < share < 1.0
+
+
+def test_fp64_warp_issue_probe():
+    """One warp issues FP64 instructions no faster than its 8 independent chains allow; more warps of
+    one block share the SM's FP64 pipe (a warp's interval grows once the pipe is full)."""
+    ctx = nbg.Context(0)
+    try:
+        one = ctx.fp64_warp_issue_cycles(1, 8)
+        many = ctx.fp64_warp_issue_cycles(8, 8)
+        with pytest.raises(nbg.NbgError):
+            ctx.fp64_warp_issue_cycles(33, 8)
+    finally:
+        ctx.close()
+    assert one > 1.0 and many >= one
