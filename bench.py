@@ -69,7 +69,7 @@ def flops_per_system_step(n):
     return per_col * 7 * n
 
 
-def build_workload(nbg, name, nsys=None, seed=0, tmax_override=0.0):
+def build_workload(nbg, name, nsys=None, seed=0, tmax_override=0.0, bodies=0):
     W = nbg.workloads
     if name == "batch_3body":
         els, h, tmax = W.batch_3body(nsys or 4096, seed)
@@ -78,7 +78,7 @@ def build_workload(nbg, name, nsys=None, seed=0, tmax_override=0.0):
         els, h, tmax = W.batch_8body(nsys or 1024, seed)
         hs, tms = [h] * len(els), [tmax] * len(els)
     elif name == "batch_uneven":
-        els, hs, tms = W.batch_uneven(nsys or 2048, seed)
+        els, hs, tms = W.batch_uneven(nsys or 2048, seed, nmin=bodies or 2, nmax=bodies or 10)
     elif name == "plain_3body":
         el, h, tmax = W.plain_3body(seed)
         els, hs, tms = [el], [h], [tmax]
@@ -512,6 +512,8 @@ def main():
     ap.add_argument("--tmax", type=float, default=0.0,
                     help="integrate every system to this tmax instead of the workload's (small profiling cases)")
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--bodies", type=int, default=0,
+                    help="batch_uneven: draw only systems of this body count (small profiling cases)")
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--serial", action="store_true", help="one stream: no producer/consumer overlap")
     ap.add_argument("--kernel-timing", default="timed", choices=["timed", "separate"],
@@ -586,7 +588,7 @@ def main():
         ctx.set_orbit_lanes(args.spw)
     ctx.set_orbit_team(args.orbit_team)
     states, timings, hs, tms, nsteps = build_workload(nbg, args.workload, args.nsys, replica_seed(args.seed, rank),
-                                                      args.tmax)
+                                                      args.tmax, args.bodies)
     total_ss = int(sum(nsteps))
     b = make_batch(nbg, states, timings, hs, tms)
     # device-resident inputs: a pristine copy and the working buffers
