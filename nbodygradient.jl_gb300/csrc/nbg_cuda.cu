@@ -478,6 +478,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
   NBG_CUDA(cudaMemsetAsync(d_bad, 0, sizeof(int), st));
   int gi = 0;
   std::vector<long long> gmaxsteps;
+  std::vector<std::vector<long long>> gsteps;  // per group, its systems' step counts, longest first
   for (auto& kv : groups) {
     GroupPlan& gp = kv.second;
     std::stable_sort(gp.systems.begin(), gp.systems.end(),
@@ -592,6 +593,8 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
       ghalf.push_back(h1);
     }
     gmaxsteps.push_back(gp.max_steps);
+    gsteps.emplace_back();
+    for (int sidx : gp.systems) gsteps.back().push_back(nsteps[sidx]);
     gi++;
   }
   NBG_CUDA(cudaGetLastError());
@@ -674,6 +677,25 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     nev += 2;
     return r;
   };
+  // The transit searches of a chunk take the team form once few of the
+  // group's systems still run (the long tail of an uneven batch, where the
+  // searches are latency-bound); while many run, one lane per search keeps
+  // every lane busy.  The same kernels' results either way (bitwise).
+  const int search_team_max = std::max(32, ctx->sm_count / 2);
+  auto search_args = [&](size_t q, const GroupArgs& g, long long c) {
+    GroupArgs gx = g;
+    const std::vector<long long>& st_q = gsteps[q];
+    const long long first = c * K;
+    // systems with steps left at this chunk: a prefix of the longest-first list
+    long long lo = 0, hi = (long long)st_q.size();
+    while (lo < hi) {
+      const long long mid = (lo + hi) / 2;
+      if (st_q[mid] > first) lo = mid + 1;
+      else hi = mid;
+    }
+    gx.search_team = (lo <= search_team_max) ? 1 : 0;
+    return gx;
+  };
   ctx->last_orbit_launches = ctx->last_jac_launches = 0;
   NBG_CUDA(cudaEventRecord(ctx->ev0, st));
   const auto host0 = std::chrono::steady_clock::now();
@@ -684,7 +706,8 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
         if (c * K >= gmaxsteps[q]) continue;
         NBG_CUDA(cudaMemsetAsync(g.task_count, 0, sizeof(int), st));
         if ((rc = timed(0, [&] { return kOrbit[g.N](g, (int)c, st); }))) return rc;
-        if (!g.notransit && (rc = timed(2, [&] { return kTransit[g.N](g, (int)c, st); }))) return rc;
+        if (!g.notransit && (rc = timed(2, [&] { return kTransit[g.N](search_args(q, g, c), (int)c, st); })))
+          return rc;
         ctx->last_launches += g.notransit ? 1 : 2;
         ctx->last_orbit_launches++;
         if (g.grad) {
@@ -735,7 +758,8 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
         NBG_CUDA(cudaEventRecord(ev_orb, sp));
         NBG_CUDA(cudaStreamWaitEvent(stt, ev_orb, 0));
         NBG_CUDA(cudaStreamWaitEvent(sw, ev_orb, 0));
-        if (!g.notransit && (rc = timed_on(stt, 2, [&] { return kTransit[g.N](g, (int)c, stt); }))) return rc;
+        if (!g.notransit && (rc = timed_on(stt, 2, [&] { return kTransit[g.N](search_args(q, g, c), (int)c, stt); })))
+          return rc;
         NBG_CUDA(cudaEventRecord(ev_tr, stt));
         ctx->last_launches += g.notransit ? 1 : 2;
         ctx->last_orbit_launches++;

@@ -563,7 +563,7 @@ int launch_jac(const GroupArgs& g, int chunk, cudaStream_t st) {
 
 template <int N>
 int launch_transit(const GroupArgs& g, int chunk, cudaStream_t st) {
-  if (team_lanes(N) > 1 && g.team && !g.kick) {
+  if (team_lanes(N) > 1 && g.team && g.search_team && !g.kick) {
     const int smem = std::max(search_team_smem_bytes<N>(), g.guard_smem);
     allow_smem(transit_team_kernel<N>, smem);
     transit_team_kernel<N><<<g.tgrid / TRANSIT_BS, TRANSIT_BS, smem, st>>>(g, chunk);

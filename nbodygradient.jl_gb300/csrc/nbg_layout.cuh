@@ -44,6 +44,11 @@ struct GroupArgs {
   int N, S, nsys, grad, K, R, npk;
   int spw;   // orbit producer: systems per warp (lanes >= spw idle)
   int team;  // orbit producer: 1 = a team of lanes per system (orbit_team_kernel), 0 = one lane
+  // transit searches of this chunk in the team form (with team != 0): set by
+  // the host per chunk when few systems of the group are still running, so
+  // that the searches are latency-bound; a full group keeps one lane per
+  // search, which uses every lane of every warp
+  int search_team;
   // Block layout of the orbit producer: pwarps independent warps per block
   // (0 or 1: one) and prod_smem bytes of dynamic shared memory per block (at
   // least what the team form needs).  A large allocation keeps the

