@@ -442,7 +442,8 @@ def measure_secondary(nbg, workload, device, seed, tune_steps):
            "launches": int(ctx.last_launch_count()),
            "autotuner": dict({k: tuning[0][k] for k in ("chunk_steps", "orbit_team", "producer_warps",
                                                           "producer_smem_kb")},
-                             predicted_ms=tuning[0]["ms"], predicted_over_measured=tuning[0]["ms"] / ms),
+                             predicted_ms=tuning[0]["ms"], predicted_over_measured=tuning[0]["ms"] / ms,
+                             trial_ms=tuning[0]["trial_ms"], trial_steps=tune_steps),
            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                         "frac": (achieved / peak) if achieved else None, "kernel": "jacobian_chunk_kernel",
                         "kernel_ms": jac_ms, "peak_source": "measured live (nbg_fp64_peak, DFMA)"},
@@ -451,6 +452,39 @@ def measure_secondary(nbg, workload, device, seed, tune_steps):
     del dev, dev0
     torch.cuda.empty_cache()
     return out
+
+
+def latency_table(nbg, device, steps=512):
+    """Single-system step latency: one batch_uneven system of each body count, `steps` gradient steps with
+    transit timing, one system per call (the one-lane and the team producer), after a warm-up call."""
+    import torch
+    W = nbg.workloads
+    out = {}
+    for n in range(2, 11):
+        els, hs, _ = W.batch_uneven(1, seed=500 + n, nmin=n, nmax=n)
+        ic = W.ic_of(els[0])
+        h = hs[0]
+        tmax = steps * h
+        row = {}
+        for team in ((0, 1) if n >= 4 else (0,)):
+            ctx = nbg.Context(device)
+            ctx.set_orbit_team(team)
+            best = None
+            for rep in range(3):
+                s = nbg.State(ic)
+                tt = nbg.TransitTiming(tmax, ic)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                nbg.Integrator(nbg.ahl21, h, 0.0, tmax)(s, tt, grad=True, ctx=ctx)
+                torch.cuda.synchronize()
+                dt = time.perf_counter() - t0
+                if rep > 0:
+                    best = dt if best is None else min(best, dt)
+            row["team" if team else "one_lane"] = best * 1e3 / steps
+            ctx.close()
+        out[str(n)] = row
+    return {"unit": "ms per grad step, one system per call (host wall time of the call)", "steps": steps,
+            "by_body_count": out}
 
 
 def measure_serving(nbg, args, capacity):
@@ -546,6 +580,8 @@ def main():
                     help="system-steps/s taken as the GPU's capacity when batch_uneven is not measured first")
     ap.add_argument("--serve-probe", type=int, default=6,
                     help="8-body 1600-day gradient requests mixed into the serving point's load stream")
+    ap.add_argument("--latency-table", action="store_true",
+                    help="print the single-system step latency for 2..10 bodies (one lane / team producer), then exit")
     ap.add_argument("--fp64-probe", action="store_true",
                     help="print the measured FP64 rates (DFMA; DMMA alone; DMMA interleaved with DFMA), then exit")
     args = ap.parse_args()
@@ -569,6 +605,9 @@ def main():
     torch.cuda.set_device(local_rank)
     if args.serve:
         run_serve(args, nbg)
+        return
+    if args.latency_table:
+        print(json.dumps({"latency_table": latency_table(nbg, local_rank)}), flush=True)
         return
     if args.fp64_probe:
         ctx = nbg.Context(local_rank)

@@ -437,9 +437,10 @@ int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double
  * the whole batch active.  For a batch of uneven length (its shortest system
  * under half its longest) two more trials run only its longest systems (at
  * most 32) for the chain's time per step, and the predicted time sums, step
- * by step, the larger of the whole-batch cost scaled by the work still
- * active and the chain cost; for an even batch it extrapolates the two
- * trials to the longest system.  The fastest candidate is kept on the
+ * by step, the time per step for the work still active: the power law
+ * through the two measured ends (the whole batch; the chain set alone),
+ * never below the chain's; for an even batch it extrapolates the two trials
+ * to the longest system.  trial_ms reports the trials' times.  The fastest candidate is kept on the
  * context (as nbg_set_tuning / nbg_set_orbit_team / nbg_set_orbit_lanes
  * would).  Arrays as for nbg_batch_integrate_transits_device.  report (may
  * be NULL) receives up to report_len candidates; *nreport (may be NULL)
@@ -450,6 +451,8 @@ typedef struct {
   int32_t producer_warps, producer_smem_kb, pad;
   double ms;                 /* predicted chunk-loop time of the full batch   */
   double system_steps_per_s; /* the batch's system-steps / that time          */
+  double trial_ms[4];        /* the trials: whole batch T and 2T steps; its
+                                longest systems alone T and 2T (0: not run)  */
 } nbg_tuning_result;
 int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc_host, double* t, double* x, double* v,
                         const double* m, double* xerror, double* verror, double* jac_step, double* jac_error,

@@ -475,8 +475,8 @@ class Batch:
             ctx.handle, self.nsys, self.descriptors(), vp("t"), vp("x"), vp("v"), vp("m"), vp("xerror"),
             vp("verror"), vp("jac_step"), vp("jac_error"), vp("dqdt"), vp("pair"), vp("jac_init"), int(trial_steps),
             rep, 32, ctypes.byref(nrep)))
-        out = [{k: getattr(rep[q], k) for k, _ in _lib.TuningResult._fields_ if k != "pad"}
-               for q in range(nrep.value)]
+        out = [{k: (list(getattr(rep[q], k)) if k == "trial_ms" else getattr(rep[q], k))
+                for k, _ in _lib.TuningResult._fields_ if k != "pad"} for q in range(nrep.value)]
         return out[:1] + sorted(out[1:], key=lambda r: r["ms"])
 
     def run_device_noalloc(self, dev_arrays, ctx=None):

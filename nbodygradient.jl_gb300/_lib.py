@@ -63,7 +63,8 @@ class DeviceInfo(ctypes.Structure):
 class TuningResult(ctypes.Structure):
     _fields_ = [("chunk_steps", ctypes.c_int32), ("orbit_team", ctypes.c_int32), ("orbit_lanes", ctypes.c_int32),
                 ("producer_warps", ctypes.c_int32), ("producer_smem_kb", ctypes.c_int32), ("pad", ctypes.c_int32),
-                ("ms", ctypes.c_double), ("system_steps_per_s", ctypes.c_double)]
+                ("ms", ctypes.c_double), ("system_steps_per_s", ctypes.c_double),
+                ("trial_ms", ctypes.c_double * 4)]
 
 
 class ServerConfig(ctypes.Structure):

@@ -1873,6 +1873,7 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
   const bool uneven = longest > 0 && (double)shortest < 0.5 * (double)longest;
   // the chain set: the longest systems (at most 32), the rest shortened to zero steps
   std::vector<nbg_system_desc> tc1(td1), tc2(td2);
+  double wchain = wtot;
   if (uneven) {
     std::vector<int> ord(nsys);
     for (int s = 0; s < nsys; s++) ord[s] = s;
@@ -1880,6 +1881,11 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
       return steps_of(desc[a].h, desc[a].tmax) > steps_of(desc[b].h, desc[b].tmax);
     });
     const int nchain = std::min(32, std::max(1, nsys / 64));
+    wchain = 0.0;
+    for (int q = 0; q < nchain; q++) {
+      const int n = desc[ord[q]].n, P = n * (n - 1) / 2;
+      wchain += 7.0 * n * (264.0 * P + 18.0 * n * n + 87.0 * n);
+    }
     for (int q = nchain; q < nsys; q++) {
       tc1[ord[q]].tmax = 0.0;
       tc2[ord[q]].tmax = 0.0;
@@ -1955,6 +1961,13 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
     if (uneven && T2 > T1) {
       const double fill = std::max(0.0, tms[0] - slope * T1);
       const double chain = std::max(0.0, (tms[3] - tms[2]) / (T2 - T1));
+      // The time per step falls from `slope` with the whole batch active to
+      // `chain` with only the chain set's work (fraction fc) left.  Fewer
+      // systems use the GPU less well, so it does not fall in proportion to
+      // the work: between the two measured ends it follows the power law
+      // through both, slope * f^a with a = log(slope / chain) / log(1 / fc).
+      const double fc = std::min(0.999, std::max(1e-9, wchain / wtot));
+      const double a = (slope > chain && chain > 0.0) ? std::log(slope / chain) / std::log(1.0 / fc) : 1.0;
       // walk the steps: between consecutive system lengths the active work is constant
       double model = fill, active = wtot;
       long long k = 0;
@@ -1962,7 +1975,8 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
       while (at < dist.size() && k < longest) {
         while (at < dist.size() && dist[at].first <= k) active -= dist[at++].second;
         const long long next = at < dist.size() ? dist[at].first : longest;
-        model += (double)(next - k) * std::max(slope * active / wtot, chain);
+        const double f = std::max(0.0, active / wtot);
+        model += (double)(next - k) * std::max(slope * std::pow(f, a), chain);
         k = next;
       }
       ms = model;
@@ -1976,6 +1990,7 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
       report[nrep].producer_smem_kb = cd.smem;
       report[nrep].ms = ms;
       report[nrep].system_steps_per_s = (double)steps / (ms * 1e-3);
+      for (int r = 0; r < 4; r++) report[nrep].trial_ms[r] = tms[r];
     }
     nrep++;
     cand_ms.push_back(ms);
