@@ -454,9 +454,10 @@ def measure_secondary(nbg, workload, device, seed, tune_steps):
     return out
 
 
-def latency_table(nbg, device, steps=512):
-    """Single-system step latency: one batch_uneven system of each body count, `steps` gradient steps with
-    transit timing, one system per call (the one-lane and the team producer), after a warm-up call."""
+def latency_table(nbg, device, steps=(256, 768)):
+    """Single-system step latency: one batch_uneven system of each body count integrated with gradient and
+    transit timing, one system per call, for two step counts; the difference of the two call times (best of 3
+    after a warm-up call) over the difference of the step counts removes the call's fixed cost."""
     import torch
     W = nbg.workloads
     out = {}
@@ -464,26 +465,29 @@ def latency_table(nbg, device, steps=512):
         els, hs, _ = W.batch_uneven(1, seed=500 + n, nmin=n, nmax=n)
         ic = W.ic_of(els[0])
         h = hs[0]
-        tmax = steps * h
         row = {}
         for team in ((0, 1) if n >= 4 else (0,)):
             ctx = nbg.Context(device)
             ctx.set_orbit_team(team)
-            best = None
-            for rep in range(3):
-                s = nbg.State(ic)
-                tt = nbg.TransitTiming(tmax, ic)
-                torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                nbg.Integrator(nbg.ahl21, h, 0.0, tmax)(s, tt, grad=True, ctx=ctx)
-                torch.cuda.synchronize()
-                dt = time.perf_counter() - t0
-                if rep > 0:
-                    best = dt if best is None else min(best, dt)
-            row["team" if team else "one_lane"] = best * 1e3 / steps
+            best = {}
+            for k in steps:
+                tmax = k * h
+                for rep in range(4):
+                    s = nbg.State(ic)
+                    tt = nbg.TransitTiming(tmax, ic)
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    nbg.Integrator(nbg.ahl21, h, 0.0, tmax)(s, tt, grad=True, ctx=ctx)
+                    torch.cuda.synchronize()
+                    dt = time.perf_counter() - t0
+                    if rep > 0:
+                        best[k] = min(best.get(k, dt), dt)
+            row["team" if team else "one_lane"] = (best[steps[1]] - best[steps[0]]) * 1e3 / (steps[1] - steps[0])
+            row["call_fixed_ms" + ("_team" if team else "")] = (best[steps[0]] * 1e3 -
+                                                                row["team" if team else "one_lane"] * steps[0])
             ctx.close()
         out[str(n)] = row
-    return {"unit": "ms per grad step, one system per call (host wall time of the call)", "steps": steps,
+    return {"unit": "ms per grad step, one system per call (difference of two call lengths)", "steps": list(steps),
             "by_body_count": out}
 
 
@@ -550,6 +554,8 @@ def main():
                     help="batch_uneven: draw only systems of this body count (small profiling cases)")
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--serial", action="store_true", help="one stream: no producer/consumer overlap")
+    ap.add_argument("--noalloc", action="store_true",
+                    help="time the allocation-free entry point (at most 128 systems) instead of the device-resident one")
     ap.add_argument("--kernel-timing", default="timed", choices=["timed", "separate"],
                     help="consumer duration from a CUDA-event pair around one launch per timed step, or from "
                          "event pairs around every launch in one extra pass")
@@ -646,7 +652,10 @@ def main():
 
     def step():
         reset()
-        b.run_device(dev, ctx)
+        if args.noalloc:
+            b.run_device_noalloc(dev, ctx)
+        else:
+            b.run_device(dev, ctx)
 
     for _ in range(args.warmup):
         step()

@@ -681,9 +681,17 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
   // group's systems still run (the long tail of an uneven batch, where the
   // searches are latency-bound); while many run, one lane per search keeps
   // every lane busy.  The same kernels' results either way (bitwise).
-  const int search_team_max = std::max(32, ctx->sm_count / 2);
-  auto search_args = [&](size_t q, const GroupArgs& g, long long c) {
-    GroupArgs gx = g;
+  //
+  // In the same tail the group's orbit producer runs on SMs of its own: its
+  // blocks ask for 210 KB of shared memory, and from the first tail chunk on
+  // every operator-record and search block asks for at least 18 KB, so that
+  // no other block fits beside a producer block (every consumer block needs
+  // 24 KB or more).  A producer warp then has its SM's FP64 pipe to itself
+  // instead of sharing it with the throughput kernels of the other groups;
+  // while many systems run, the layout stays the autotuner's.
+  const int tail_max = std::max(32, ctx->sm_count / 2);
+  bool tail_any = false;
+  auto active_at = [&](size_t q, long long c) -> long long {
     const std::vector<long long>& st_q = gsteps[q];
     const long long first = c * K;
     // systems with steps left at this chunk: a prefix of the longest-first list
@@ -693,7 +701,22 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
       if (st_q[mid] > first) lo = mid + 1;
       else hi = mid;
     }
-    gx.search_team = (lo <= search_team_max) ? 1 : 0;
+    return lo;
+  };
+  auto search_args = [&](size_t q, const GroupArgs& g, long long c) {
+    GroupArgs gx = g;
+    gx.search_team = (active_at(q, c) <= tail_max) ? 1 : 0;
+    if (tail_any) gx.guard_smem = std::max(gx.guard_smem, 18 * 1024);
+    return gx;
+  };
+  auto orbit_args = [&](size_t q, const GroupArgs& g, long long c) {
+    GroupArgs gx = g;
+    if (active_at(q, c) <= tail_max) gx.prod_smem = std::max(gx.prod_smem, 210 * 1024);
+    return gx;
+  };
+  auto ops_args = [&](const GroupArgs& g) {
+    GroupArgs gx = g;
+    if (tail_any) gx.guard_smem = std::max(gx.guard_smem, 18 * 1024);
     return gx;
   };
   ctx->last_orbit_launches = ctx->last_jac_launches = 0;
@@ -754,7 +777,8 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
           return rc;
         if (c >= 2) NBG_CUDA(cudaStreamWaitEvent(sp, ev_done, 0));
         NBG_CUDA(cudaMemsetAsync(g.task_count, 0, sizeof(int), sp));
-        if ((rc = timed_on(sp, 0, [&] { return kOrbit[g.N](g, (int)c, sp); }))) return rc;
+        if (active_at(q, c) <= tail_max) tail_any = true;
+        if ((rc = timed_on(sp, 0, [&] { return kOrbit[g.N](orbit_args(q, g, c), (int)c, sp); }))) return rc;
         NBG_CUDA(cudaEventRecord(ev_orb, sp));
         NBG_CUDA(cudaStreamWaitEvent(stt, ev_orb, 0));
         NBG_CUDA(cudaStreamWaitEvent(sw, ev_orb, 0));
@@ -764,7 +788,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
         ctx->last_launches += g.notransit ? 1 : 2;
         ctx->last_orbit_launches++;
         if (g.grad) {
-          if ((rc = timed_on(sw, 3, [&] { return kOps[g.N](g, (int)c, sw); }))) return rc;
+          if ((rc = timed_on(sw, 3, [&] { return kOps[g.N](ops_args(g), (int)c, sw); }))) return rc;
           NBG_CUDA(cudaStreamWaitEvent(sw, ev_tr, 0));
           sample_now = (c == ((gmaxsteps[q] + K - 1) / K) / 2);
           sampled += (ctx->profile == 3 && sample_now) ? 1 : 0;
