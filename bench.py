@@ -466,7 +466,7 @@ def latency_table(nbg, device, steps=(256, 768)):
         ic = W.ic_of(els[0])
         h = hs[0]
         row = {}
-        for team in ((0, 1) if n >= 4 else (0,)):
+        for team in ((0, 1, 2) if n >= 4 else (0, 2)):
             ctx = nbg.Context(device)
             ctx.set_orbit_team(team)
             best = {}
@@ -482,9 +482,9 @@ def latency_table(nbg, device, steps=(256, 768)):
                     dt = time.perf_counter() - t0
                     if rep > 0:
                         best[k] = min(best.get(k, dt), dt)
-            row["team" if team else "one_lane"] = (best[steps[1]] - best[steps[0]]) * 1e3 / (steps[1] - steps[0])
-            row["call_fixed_ms" + ("_team" if team else "")] = (best[steps[0]] * 1e3 -
-                                                                row["team" if team else "one_lane"] * steps[0])
+            name = {0: "one_lane", 1: "team", 2: "wide"}[team]
+            row[name] = (best[steps[1]] - best[steps[0]]) * 1e3 / (steps[1] - steps[0])
+            row["call_fixed_ms_" + name] = best[steps[0]] * 1e3 - row[name] * steps[0]
             ctx.close()
         out[str(n)] = row
     return {"unit": "ms per grad step, one system per call (difference of two call lengths)", "steps": list(steps),
@@ -561,7 +561,8 @@ def main():
                          "event pairs around every launch in one extra pass")
     ap.add_argument("--spw", type=int, default=0, help="orbit producer systems per warp (0 = automatic)")
     ap.add_argument("--orbit-team", type=int, default=-1,
-                    help="orbit producer form: -1 automatic, 0 one lane per system, 1 a team per system")
+                    help="orbit producer form: -1 automatic, 0 one lane per system, 1 a team per system, 2 the wide "
+                         "team form, 3 a team, wide when latency-bound")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip the autotuner (it picks chunk length and orbit-producer mapping before the warm-up)")
@@ -753,8 +754,9 @@ def main():
                        "chunk_steps": chunk,
                        "orbit_systems_per_warp": (args.spw or "auto") if tuning is None
                        else (tuning[0]["orbit_lanes"] or "auto"),
-                       "orbit_team": ({-1: "auto", 0: "off", 1: "on"}[args.orbit_team] if tuning is None
-                                      else {0: "off", 1: "on"}[tuning[0]["orbit_team"]]),
+                       "orbit_team": ({-1: "auto", 0: "off", 1: "on", 2: "wide", 3: "on, wide when latency-bound"}
+                                      [args.orbit_team] if tuning is None
+                                      else {0: "off", 1: "on, wide when latency-bound"}[tuning[0]["orbit_team"]]),
                        "autotuner": None if tuning is None else {
                            "trial_steps_per_system": args.tune_steps,
                            "chosen": {k: tuning[0][k] for k in ("chunk_steps", "orbit_team", "producer_warps",

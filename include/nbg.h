@@ -465,12 +465,19 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc_
 int nbg_set_orbit_lanes(nbg_context* ctx, int systems_per_warp);
 
 /* Form of the orbit producer for groups without kick pairs: -1 automatic
- * (default: a team of N/2 lanes per system from N = 5 on), 0 one lane per
- * system, 1 a team for every N.  A team runs the Kepler sweeps and
- * phisalpha!'s pair loops level by level (pairs with equal i + j share no
- * body and run in parallel), which keeps every body's sequence of updates
- * and so gives bitwise the same results.  A tuning knob; no counterpart in
- * the reference. */
+ * (default: one lane per system up to four bodies and a team of N/2 lanes
+ * per system from N = 5 on, each in its wide form in latency-bound chunks),
+ * 0 one lane per system, 1 a team for every N, 2 the wide team form for
+ * every N, 3 a team for every N, wide in latency-bound chunks.  A team runs
+ * the Kepler sweeps and phisalpha!'s pair loops level by level (pairs with
+ * equal i + j share no body and run in parallel), which keeps every body's
+ * sequence of updates and so gives bitwise the same results.  The wide form
+ * runs each pair solve on two lanes, each evaluating one of its independent
+ * parts (the sine and cosine series, the Newton update's numerator and
+ * denominator, G3 and H1): bitwise the same results with fewer FP64
+ * instructions on the system's warp.  A chunk is latency-bound when at most
+ * max(32, SMs / 2) of its group's systems still run.  A tuning knob; no
+ * counterpart in the reference. */
 int nbg_set_orbit_team(nbg_context* ctx, int mode);
 
 /* Block layout of the orbit producer (a tuning knob; no counterpart in the

@@ -360,9 +360,18 @@ namespace nbg {
 // Team producer (a team of lanes per system) for kick-free groups: automatic
 // from five bodies on, where the level-parallel sweeps shorten the step's
 // critical path by 1.4x (N = 5) to 2.6x (N = 10).
+// Modes (nbg_set_orbit_team): -1 automatic, 0 one lane, 1 team, 2 wide
+// team always, 3 team with the wide form in latency-bound chunks.
 bool use_team(int mode, int N, unsigned long long kick) {
   if (kick) return false;
   return mode > 0 || (mode < 0 && N >= 5);
+}
+
+// The wide team form (two lanes per pair solve): always in mode 2, in the
+// latency-bound chunks (few systems running) in modes -1 and 3.
+bool use_wide(int mode, bool latency_bound, unsigned long long kick) {
+  if (kick) return false;
+  return mode == 2 || ((mode < 0 || mode == 3) && latency_bound);
 }
 }  // namespace nbg
 
@@ -711,7 +720,9 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
   };
   auto orbit_args = [&](size_t q, const GroupArgs& g, long long c) {
     GroupArgs gx = g;
-    if (active_at(q, c) <= tail_max) gx.prod_smem = std::max(gx.prod_smem, 210 * 1024);
+    const bool tail = active_at(q, c) <= tail_max;
+    if (tail) gx.prod_smem = std::max(gx.prod_smem, 210 * 1024);
+    gx.wide = use_wide(ctx->orbit_team, tail, g.kick) ? 1 : 0;
     return gx;
   };
   auto ops_args = [&](const GroupArgs& g) {
@@ -728,7 +739,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
         const GroupArgs& g = gargs[q];
         if (c * K >= gmaxsteps[q]) continue;
         NBG_CUDA(cudaMemsetAsync(g.task_count, 0, sizeof(int), st));
-        if ((rc = timed(0, [&] { return kOrbit[g.N](g, (int)c, st); }))) return rc;
+        if ((rc = timed(0, [&] { return kOrbit[g.N](orbit_args(q, g, c), (int)c, st); }))) return rc;
         if (!g.notransit && (rc = timed(2, [&] { return kTransit[g.N](search_args(q, g, c), (int)c, st); })))
           return rc;
         ctx->last_launches += g.notransit ? 1 : 2;
@@ -1365,7 +1376,7 @@ int nbg_set_producer_layout(nbg_context* ctx, int warps_per_block, int smem_kb, 
 
 int nbg_set_orbit_team(nbg_context* ctx, int mode) {
   if (!ctx) return set_error(NBG_EINVAL, "ctx is NULL");
-  if (mode < -1 || mode > 1) return set_error(NBG_EINVAL, "mode = %d not in -1..1", mode);
+  if (mode < -1 || mode > 3) return set_error(NBG_EINVAL, "mode = %d not in -1..3", mode);
   ctx->orbit_team = mode;
   return NBG_OK;
 }
@@ -1963,7 +1974,7 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
   for (size_t q = 0; q <= cands.size(); q++) {
     const Cand& cd = cands[q == 0 ? 0 : q - 1];  // the first candidate runs twice: the first run allocates
     ctx->chunk_steps = cd.chunk;
-    ctx->orbit_team = cd.team;
+    ctx->orbit_team = cd.team ? 3 : 0;  // a team, wide in latency-bound chunks
     ctx->orbit_spw = cd.spw;
     ctx->prod_warps = cd.pw;
     ctx->prod_smem_kb = cd.smem;
@@ -2036,7 +2047,7 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
     return rc ? rc : set_error(NBG_EINVAL, "autotune: no candidate ran");
   }
   ctx->chunk_steps = cands[best].chunk;
-  ctx->orbit_team = cands[best].team;
+  ctx->orbit_team = cands[best].team ? 3 : 0;
   ctx->orbit_spw = cands[best].spw;
   ctx->prod_warps = cands[best].pw;
   ctx->prod_smem_kb = cands[best].smem;

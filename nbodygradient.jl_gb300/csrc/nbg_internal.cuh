@@ -31,6 +31,7 @@ double check_step(double t0, double tmax);
 // Whether a group of N bodies with kick-pair mask `kick` uses the team form
 // of the orbit producer (mode: -1 automatic, 0 never, 1 whenever possible).
 bool use_team(int mode, int N, unsigned long long kick);
+bool use_wide(int mode, bool latency_bound, unsigned long long kick);
 
 // Kernel launchers for body count N (nbg_inst.cu instantiates the kernels).
 int launch_group_orbit(int N, const GroupArgs& g, int chunk, cudaStream_t st);

@@ -254,6 +254,151 @@ __device__ __noinline__ void kep_delxv(const double* x0, const double* v0, doubl
   P.H1v = gh.h1; P.H2v = gh.h2; P.H3v = gh.h3; P.H5v = gh.h5; P.H6v = gh.h6;
 }
 
+// ---------------------------------------------------------------- two lanes
+// The wide form of the team producer runs each pair solve on two adjacent
+// lanes of one warp (role 0 and role 1; `mask` names both, `base` is role
+// 0's lane).  Both lanes execute the same instructions.  Where the solve has
+// two independent pieces of FP64 work of one shape -- the sin and cos
+// series, the Newton update's numerator and denominator, G3 and H1 -- each
+// lane evaluates one of them with its own coefficients or operands, and a
+// shuffle (no FP64 instruction) hands each result to both.  Every value is
+// formed by the same operations in the same order as in kep_delxv, so the
+// results are bitwise the same.  A warp issues one FP64 instruction per 64
+// cycles however many of them are independent, so one system's step takes
+// as long as the FP64 instructions its warp issues; splitting them over two
+// lanes removes about a fifth of a drift solve's.
+
+// sincos_kepler on two lanes: role 0 evaluates the sine series, role 1 the
+// cosine series; both lanes receive both.
+__device__ __forceinline__ void sincos_kepler2(double x, double* s, double* c, int role, unsigned mask, int base) {
+  if (fabs(x) > 0.78539816339744831) {
+    sincos(x, s, c);
+    return;
+  }
+  const double x2 = x * x;
+  double p = role ? -0x1.6827863b97d97p-53 : 0x1.952c77030ad4ap-49;
+  p = fma(p, x2, role ? 0x1.ae7f3e733b81fp-45 : -0x1.ae7f3e733b81fp-41);
+  p = fma(p, x2, role ? -0x1.93974a8c07c9dp-37 : 0x1.6124613a86d09p-33);
+  p = fma(p, x2, role ? 0x1.1eed8eff8d898p-29 : -0x1.ae64567f544e4p-26);
+  p = fma(p, x2, role ? -0x1.27e4fb7789f5cp-22 : 0x1.71de3a556c734p-19);
+  p = fma(p, x2, role ? 0x1.a01a01a01a01ap-16 : -0x1.a01a01a01a01ap-13);
+  p = fma(p, x2, role ? -0x1.6c16c16c16c17p-10 : 0x1.1111111111111p-7);
+  p = fma(p, x2, role ? 0x1.5555555555555p-5 : -0x1.5555555555555p-3);
+  const double b = x2 * (role ? x2 : x);  // x x2 (sine) or x2 x2 (cosine)
+  const double one_minus = fma(-0.5, x2, 1.0);
+  const double v = fma(b, p, role ? one_minus : x);
+  *s = __shfl_sync(mask, v, base);
+  *c = __shfl_sync(mask, v, base + 1);
+}
+
+// kep_delxv<DRIFT_FIRST, false> on two lanes (see above); both lanes return
+// the same delxv and P.
+template <bool DRIFT_FIRST>
+__device__ __noinline__ void kep_delxv2(const double* x0, const double* v0, double k, double h, double* delxv,
+                                        KepParams& P, int role, unsigned mask, int base) {
+  double rt0 = x0[0] - h * v0[0], rt1 = x0[1] - h * v0[1], rt2 = x0[2] - h * v0[2];
+  double r0 = DRIFT_FIRST ? sqrt(rt0 * rt0 + rt1 * rt1 + rt2 * rt2) : sqrt(x0[0] * x0[0] + x0[1] * x0[1] + x0[2] * x0[2]);
+  double r0inv = 1.0 / r0;
+  double beta0 = 2.0 * k * r0inv - (v0[0] * v0[0] + v0[1] * v0[1] + v0[2] * v0[2]);
+  double beta0inv = 1.0 / beta0;
+  double signb = jsign(beta0);
+  double sqb = sqrt(signb * beta0);
+  double zeta = k - r0 * beta0;
+  double eta = DRIFT_FIRST ? (rt0 * v0[0] + rt1 * v0[1] + rt2 * v0[2]) : (x0[0] * v0[0] + x0[1] * v0[1] + x0[2] * v0[2]);
+  double gamma_guess;
+  if (zeta != 0.0) {
+    double zinv = 6.0 / zeta;
+    gamma_guess = cubic1(0.5 * eta * sqb * zinv, r0 * signb * beta0 * zinv, (-h) * signb * beta0 * sqb * zinv);
+  } else if (eta != 0.0) {
+    double reta = r0 / eta;
+    double disc = reta * reta + 2.0 * h / eta;
+    gamma_guess = (disc > 0.0) ? sqb * ((-reta) + sqrt(disc)) : h * r0inv * sqb;
+  } else {
+    gamma_guess = h * r0inv * sqb;
+  }
+  double gamma = gamma_guess;
+  double gamma1 = 2.0 * gamma, gamma2 = 3.0 * gamma;
+  double c2 = -2.0 * zeta, c3 = 2.0 * eta * signb * sqb, c4 = (-sqb) * h * beta0, c5 = 2.0 * eta * signb * sqb;
+  // the update's numerator k gamma + c2 sx cx + c3 sx^2 + c4 (role 0) and
+  // denominator 2 signb zeta sx^2 + c5 sx cx + r0 beta0 (role 1), term by term
+  const double kz = 2.0 * signb * zeta, rb = r0 * beta0;
+  const double a1 = role ? kz : k, a2 = role ? c5 : c2, a3 = role ? 1.0 : c3, a4 = role ? 0.0 : c4;
+  double sx, cx;
+  int iter = 0;
+  while (iter < 20) {
+    gamma2 = gamma1;
+    gamma1 = gamma;
+    double xx = 0.5 * gamma;
+    if (beta0 > 0.0) {
+      sincos_kepler2(xx, &sx, &cx, role, mask, base);
+    } else {
+      sx = sinh(xx);
+      cx = exp(-xx) + sx;
+    }
+    const double ss = sx * sx;
+    double acc = a1 * (role ? ss : gamma) + (a2 * sx) * cx;
+    acc = acc + a3 * (role ? rb : ss);  // 1.0 * (r0 beta0) is r0 beta0 exactly
+    const double acc4 = acc + a4;
+    acc = role ? acc : acc4;
+    const double num = __shfl_sync(mask, acc, base);
+    const double den = __shfl_sync(mask, acc, base + 1);
+    gamma = gamma - num / den;
+    iter += 1;
+    if (gamma == gamma2 || gamma == gamma1) break;
+  }
+  P.newton_iter = iter;
+  double xx = 0.5 * gamma;
+  if (beta0 > 0.0) {
+    sincos_kepler2(xx, &sx, &cx, role, mask, base);
+  } else {
+    sx = sinh(xx);
+    cx = exp(-xx) + sx;
+  }
+  double g1bs = 2.0 * sx * cx / sqb;
+  double g2bs = 2.0 * signb * (sx * sx) * beta0inv;
+  double g0bs = 1.0 - beta0 * g2bs;
+  GH gh;
+  if (DRIFT_FIRST) {
+    gh = gh_functions<GH_G3>(gamma, beta0, sqb);
+  } else if (gamma < 0.5) {
+    // G3 (role 0) and H1 (role 1) as gh_functions forms them; H2 on both
+    const double x2 = (-jsign(beta0)) * (gamma * gamma);
+    const double poly = gh_horner(kGHCoef[role ? 1 : 0], x2);
+    const double pn = (role ? x2 : -x2) * (role ? x2 : gamma);          // (-x2) gamma | x2 x2
+    const double pd = ((role ? beta0 : 6.0) * beta0) * (role ? 12.0 : sqb);  // (6 beta) sqb | 12 (beta beta)
+    const double v = poly * (pn / pd);
+    gh.g3 = __shfl_sync(mask, v, base);
+    gh.h1 = __shfl_sync(mask, v, base + 1);
+    gh.h2 = gh_horner(kGHCoef[2], x2) * (((-x2) * gamma) / ((3.0 * beta0) * sqb));
+    gh.h3 = gh.h5 = gh.h6 = 0.0;
+  } else {
+    gh = gh_functions<GH_G3 | GH_H1 | GH_H2>(gamma, beta0, sqb);
+  }
+  double g3bs = gh.g3;
+  double h1 = 0.0, h2 = 0.0;
+  double r = r0 * g0bs + eta * g1bs + k * g2bs;
+  double rinv = 1.0 / r;
+  double dfdt = (-k) * g1bs * rinv * r0inv;
+  double fm1, gmh, dgdtm1;
+  if (DRIFT_FIRST) {
+    fm1 = (-k) * r0inv * g2bs;
+    gmh = k * r0inv * (h * g2bs - r0 * g3bs);
+    dgdtm1 = k * r0inv * rinv * (h * g1bs - r0 * g2bs);
+  } else {
+    h1 = gh.h1;
+    h2 = gh.h2;
+    fm1 = k * rinv * (g2bs - k * r0inv * h1);
+    gmh = k * rinv * (r0 * h2 + eta * h1);
+    dgdtm1 = (-k) * rinv * g2bs;
+  }
+  for (int j = 0; j < 3; j++) delxv[j] = fm1 * x0[j] + gmh * v0[j];
+  for (int j = 0; j < 3; j++) delxv[3 + j] = dfdt * x0[j] + dgdtm1 * v0[j];
+  P.gamma = gamma; P.g0 = g0bs; P.g1 = g1bs; P.g2 = g2bs; P.g3 = g3bs; P.h1 = h1; P.h2 = h2;
+  P.dfdt = dfdt; P.fm1 = fm1; P.gmh = gmh; P.dgdtm1 = dgdtm1; P.r0 = r0; P.r = r; P.r0inv = r0inv; P.rinv = rinv;
+  P.k = k; P.h = h; P.beta = beta0; P.betainv = beta0inv; P.eta = eta; P.sqb = sqb; P.zeta = zeta;
+  P.H1v = gh.h1; P.H2v = gh.h2; P.H3v = gh.h3; P.H5v = gh.h5; P.H6v = gh.h6;
+}
+
 // compute_jacobian_gamma! (ahl21.jl:896-1139, debug = false).  jk is the 6x8
 // jac_kepler (col-major: jk[row + 6 col]); jm the 6-vector jac_mass.
 template <bool DRIFT_FIRST>

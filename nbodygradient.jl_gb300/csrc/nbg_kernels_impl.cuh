@@ -538,6 +538,13 @@ inline void allow_smem(K kernel, int bytes) {
 template <int N>
 int launch_orbit(const GroupArgs& g, int chunk, cudaStream_t st) {
   const int W = g.pwarps > 0 ? g.pwarps : 1;
+  if (g.wide && !g.kick) {
+    constexpr int T = PROD_BS / (2 * team_lanes(N));
+    const int smem = std::max(team_smem_bytes<N, 2>(W), g.prod_smem);
+    allow_smem(orbit_team_kernel<N, 2>, smem);
+    orbit_team_kernel<N, 2><<<(g.S + W * T - 1) / (W * T), PROD_BS * W, smem, st>>>(g, chunk);
+    return 0;
+  }
   if (g.team && !g.kick) {
     constexpr int T = PROD_BS / team_lanes(N);
     const int smem = std::max(team_smem_bytes<N>(W), g.prod_smem);

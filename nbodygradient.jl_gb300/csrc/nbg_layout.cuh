@@ -49,6 +49,10 @@ struct GroupArgs {
   // that the searches are latency-bound; a full group keeps one lane per
   // search, which uses every lane of every warp
   int search_team;
+  // orbit producer in the wide team form (two lanes per pair solve,
+  // orbit_team_kernel<N, 2>) for this chunk: set by the host for latency-bound
+  // chunks (few systems running) of groups without kick pairs
+  int wide;
   // Block layout of the orbit producer: pwarps independent warps per block
   // (0 or 1: one) and prod_smem bytes of dynamic shared memory per block (at
   // least what the team form needs).  A large allocation keeps the

@@ -78,23 +78,73 @@ __device__ __forceinline__ bool level_pair(int lev, int t, int* i, int* j) {
   return true;
 }
 
+// kepler_pair<N, DRIFT_FIRST, false, false> on the two lanes of a pair slot
+// (kep_delxv2): both lanes read the pair's coordinates and solve it; role 0
+// then updates body i and writes the first half of the capture, role 1 body
+// j and the rest.  x_i and x_j are separate variables, so splitting their
+// updates between the lanes changes no value.
+template <int N, bool DRIFT_FIRST>
+__device__ __forceinline__ void kepler_pair_w2(Sys<N>& s, int i, int j, double h2, const Rec& cap, int coff,
+                                               int role, unsigned mask, int base) {
+  double x0[3], v0[3];
+  for (int k = 0; k < 3; k++) {
+    x0[k] = s.x[3 * i + k] - s.x[3 * j + k];
+    v0[k] = s.v[3 * i + k] - s.v[3 * j + k];
+  }
+  const double gm = GNEWT * (s.m[i] + s.m[j]);
+  __syncwarp(mask);  // both lanes have read the pair before either writes
+  if (cap.p && gm == 0.0 && role == 0) cap.put(coff + 6 + 15, 0.0);
+  if (gm != 0.0) {
+    KepParams P;
+    double delxv[6];
+    kep_delxv2<DRIFT_FIRST>(x0, v0, gm, h2, delxv, P, role, mask, base);
+    if (cap.p) {
+      const double pv[22] = {P.gamma, P.g0, P.g1, P.g2, P.g3, P.h1, P.h2, P.dfdt, P.fm1, P.gmh, P.dgdtm1,
+                             P.r0, P.r, P.r0inv, P.rinv, P.k, P.h, P.beta, P.betainv, P.eta, P.sqb, P.zeta};
+      if (role == 0) {
+        for (int q = 0; q < 3; q++) {
+          cap.put(coff + q, x0[q]);
+          cap.put(coff + 3 + q, v0[q]);
+        }
+        for (int q = 0; q < 8; q++) cap.put(coff + 6 + q, pv[q]);
+      } else {
+        for (int q = 8; q < 22; q++) cap.put(coff + 6 + q, pv[q]);
+      }
+    }
+    const double mijinv = 1.0 / (s.m[i] + s.m[j]);
+    const double mi = s.m[i] * mijinv, mj = s.m[j] * mijinv;
+    const int b = role ? j : i;
+    const double f = role ? (-mi) : mj;
+    for (int k = 0; k < 3; k++) kahan(s.x[3 * b + k], s.xe[3 * b + k], f * delxv[k]);
+    for (int k = 0; k < 3; k++) kahan(s.v[3 * b + k], s.ve[3 * b + k], f * delxv[3 + k]);
+  }
+}
+
 // One AHL21 step without gradient operators for a group with no kick pairs
-// (ahl21_no_grad.jl:6-18 order), run by the L lanes of a team; `run` is false
-// for lanes whose system does not step (they still meet every __syncwarp).
-// cap / xs as in ahl21_step.  a: the team's 3N acceleration scratch.
-template <int N>
+// (ahl21_no_grad.jl:6-18 order), run by the R * L lanes of a team (R = 2:
+// each pair slot p on two lanes, roles 0 and 1, kepler_pair_w2); `run` is
+// false for lanes whose system does not step (they still meet every
+// __syncwarp).  cap / xs as in ahl21_step.  a: the team's 3N acceleration
+// scratch.
+template <int N, int R = 1>
 __device__ __forceinline__ void team_step(Sys<N>& s, double* a, Work<N>& w, int t, bool run, double h,
                                           const Rec& cap, const Rec& xs) {
-  constexpr int L = team_lanes(N);
+  constexpr int L = R * team_lanes(N);
   constexpr int P = N * (N - 1) / 2;
+  const int p = t / R, role = t % R;
+  const int lane = threadIdx.x & 31;
+  const int base = lane - role;
+  const unsigned mask = (R == 2) ? (3u << base) : 0u;
   const double h2 = 0.5 * h;
   if (run)
     for (int q = t; q < 3 * N; q += L) kahan(s.x[q], s.xe[q], h2 * s.v[q]);
   __syncwarp();
   for (int lev = 1; lev <= 2 * N - 3; lev++) {
     int i, j;
-    if (run && level_pair<N>(lev, t, &i, &j))
-      kepler_pair<N, true, false, false>(s, w, i, j, h2, Rec{nullptr, 0}, 0, cap, pair_bit(i, j, N) * PCAP);
+    if (run && level_pair<N>(lev, p, &i, &j)) {
+      if (R == 1) kepler_pair<N, true, false, false>(s, w, i, j, h2, Rec{nullptr, 0}, 0, cap, pair_bit(i, j, N) * PCAP);
+      else kepler_pair_w2<N, true>(s, i, j, h2, cap, pair_bit(i, j, N) * PCAP, role, mask, base);
+    }
     __syncwarp();
   }
   if (run) {
@@ -106,19 +156,21 @@ __device__ __forceinline__ void team_step(Sys<N>& s, double* a, Work<N>& w, int 
   const double coeff = 2.0 * (h * h * h) / 96.0 * 2.0 * GNEWT;  // alpha = 2 (ahl21.jl:47)
   for (int lev = 1; lev <= 2 * N - 3; lev++) {
     int i, j;
-    if (run && level_pair<N>(lev, t, &i, &j)) phis_accel_pair<N>(s, a, i, j);
+    if (run && role == 0 && level_pair<N>(lev, p, &i, &j)) phis_accel_pair<N>(s, a, i, j);
     __syncwarp();
   }
   for (int lev = 1; lev <= 2 * N - 3; lev++) {
     int i, j;
-    if (run && level_pair<N>(lev, t, &i, &j)) phis_kick_pair<N>(s, a, i, j, coeff);
+    if (run && role == 0 && level_pair<N>(lev, p, &i, &j)) phis_kick_pair<N>(s, a, i, j, coeff);
     __syncwarp();
   }
   for (int lev = 2 * N - 3; lev >= 1; lev--) {
     int i, j;
-    if (run && level_pair<N>(lev, t, &i, &j))
-      kepler_pair<N, false, false, false>(s, w, i, j, h2, Rec{nullptr, 0}, 0, cap,
-                                          (P + (P - 1 - pair_bit(i, j, N))) * PCAP);
+    if (run && level_pair<N>(lev, p, &i, &j)) {
+      const int coff = (P + (P - 1 - pair_bit(i, j, N))) * PCAP;
+      if (R == 1) kepler_pair<N, false, false, false>(s, w, i, j, h2, Rec{nullptr, 0}, 0, cap, coff);
+      else kepler_pair_w2<N, false>(s, i, j, h2, cap, coff, role, mask, base);
+    }
     __syncwarp();
   }
   if (run)
@@ -128,18 +180,20 @@ __device__ __forceinline__ void team_step(Sys<N>& s, double* a, Work<N>& w, int 
 
 // Dynamic shared memory the team producer needs for W warps per block:
 // per team a Sys<N>, 3N accelerations, N g values and N transit counts.
-template <int N>
+template <int N, int R = 1>
 __host__ __device__ constexpr int team_smem_bytes(int W) {
-  return W * (PROD_BS / team_lanes(N)) * (int)(sizeof(Sys<N>) + (3 * N + N) * sizeof(double) + N * sizeof(long long));
+  return W * (PROD_BS / (R * team_lanes(N))) *
+         (int)(sizeof(Sys<N>) + (3 * N + N) * sizeof(double) + N * sizeof(long long));
 }
 
-// Orbit producer, team form: L lanes per system, T = 32 / L systems per warp
-// (lanes beyond T * L idle), pwarps independent warps per block.  Same
+// Orbit producer, team form: L = R * team_lanes(N) lanes per system
+// (R = 2: the wide form, two lanes per pair solve), T = 32 / L systems per
+// warp (lanes beyond T * L idle), pwarps independent warps per block.  Same
 // inputs, outputs and arithmetic as orbit_chunk_kernel<N> for groups
 // without kick pairs.
-template <int N>
+template <int N, int R = 1>
 __global__ void __launch_bounds__(PROD_BS * PROD_MAX_WARPS) orbit_team_kernel(GroupArgs g, int chunk) {
-  constexpr int L = team_lanes(N);
+  constexpr int L = R * team_lanes(N);
   constexpr int T = PROD_BS / L;
   const int W = g.pwarps > 0 ? g.pwarps : 1;
   extern __shared__ double team_smem[];
@@ -194,7 +248,7 @@ __global__ void __launch_bounds__(PROD_BS * PROD_MAX_WARPS) orbit_team_kernel(Gr
         rx[3 * N + q] = st.v[q];
       }
     }
-    team_step<N>(st, acc[tm], w, t, run && !last, hs, cap, xs);
+    team_step<N, R>(st, acc[tm], w, t, run && !last, hs, cap, xs);
     // the last step also forms dq/dt: the one-lane step, on the team's first lane
     if (last && t == 0) ahl21_step<N, true, true>(st, w, hs, 0, Rec{nullptr, 0}, cap, xs);
     __syncwarp();

@@ -615,7 +615,12 @@ int service_group(nbg_server* srv, int gi) {
   // searches on stt beside the operator records on sw, then the consumer
   NBG_CUDA(cudaMemsetAsync(gc.task_count, 0, sizeof(int), st));
   int rc;
-  if ((rc = launch_group_orbit(N, gc, (int)c, st))) return rc;
+  {
+    // the wide team form while few slots are running (latency-bound chunks)
+    GroupArgs go = gc;
+    go.wide = use_wide(srv->cfg.orbit_team, G->active <= std::max(32, srv->sm_count / 2), G->kick) ? 1 : 0;
+    if ((rc = launch_group_orbit(N, go, (int)c, st))) return rc;
+  }
   NBG_CUDA(cudaEventRecord(G->ev_orb[par], st));
   NBG_CUDA(cudaStreamWaitEvent(stt, G->ev_orb[par], 0));
   NBG_CUDA(cudaStreamWaitEvent(sw, G->ev_orb[par], 0));

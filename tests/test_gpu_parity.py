@@ -288,17 +288,18 @@ def test_batch_matches_oracle():
 
 @pytest.mark.parametrize("grad", [True, False])
 def test_team_producer_is_bitwise_the_one_lane_producer(grad):
-    """The team form of the orbit producer (level-parallel sweeps) against the
-    one-lane form, and both in multi-warp blocks holding their SM's shared
-    memory, for every body count: bitwise the same x, v, jac_step, transit
-    times and derivatives."""
+    """The team form of the orbit producer (level-parallel sweeps) and its wide
+    form (two lanes per pair solve) against the one-lane form, all in
+    multi-warp blocks holding their SM's shared memory too, for every body
+    count: bitwise the same x, v, jac_step, transit times and derivatives."""
     specs = []
     for n in range(2, 11):
         els, hs, tms = W.batch_uneven(3, seed=40 + n, nmin=n, nmax=n)
         specs += [(el, h, 90 * h, grad) for el, h in zip(els, hs)]
     states, timings, hs, tms, grads = _batch_inputs(specs)
     out = []
-    for mode, layout in ((0, (1, 0, 0)), (1, (1, 0, 0)), (0, (4, 200, 32)), (1, (4, 200, 32)), (1, (3, 0, 0))):
+    for mode, layout in ((0, (1, 0, 0)), (1, (1, 0, 0)), (0, (4, 200, 32)), (1, (4, 200, 32)), (1, (3, 0, 0)),
+                         (2, (1, 0, 0)), (2, (4, 200, 32))):
         ctx = nbg.Context(0)
         ctx.set_orbit_team(mode)
         ctx.set_producer_layout(*layout)
