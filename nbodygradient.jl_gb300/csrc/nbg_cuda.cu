@@ -275,6 +275,9 @@ struct nbg_context {
   // overlap mode: per group q, a producer stream, an operator / Jacobian
   // stream and a transit-search stream (gstreams[3q .. 3q+2])
   std::vector<cudaStream_t> gstreams;
+  // the same for the groups of a batch whose systems run longest: streams of
+  // the device's highest priority (their blocks are dispatched first)
+  std::vector<cudaStream_t> hstreams;
   std::vector<cudaEvent_t> sync_events;  // cross-stream ordering, no timing
   NoallocPlan* noalloc = nullptr;         // host plan of the allocation-free entry point
 
@@ -766,22 +769,46 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     // throughput-bound operator and Jacobian kernels.  With a stream triple of
     // its own, every group (body count, grad, pair pattern) progresses
     // independently: its chunk chain is not held up by another group's.
+    //
+    // In a batch of several groups, the groups whose longest chain is at
+    // least half the batch's longest get streams of the highest priority:
+    // their blocks are dispatched before the other groups' as SMs free up, so
+    // that the long chains' pipelines are not held back by the short groups'
+    // throughput work (the results do not depend on it).  A chain's length
+    // is its longest system's steps times 2N - 3, the pair solves on the
+    // critical path of a team step.
     const size_t ng = gargs.size();
-    while (ctx->gstreams.size() < 3 * ng) {
-      cudaStream_t s2;
-      NBG_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
-      ctx->gstreams.push_back(s2);
+    auto chain_len = [&](size_t q) { return (double)gmaxsteps[q] * (2.0 * gargs[q].N - 3.0); };
+    double longest_all = 0.0;
+    for (size_t q = 0; q < ng; q++) longest_all = std::max(longest_all, chain_len(q));
+    std::vector<cudaStream_t> gstr(3 * ng);
+    {
+      size_t nlo = 0, nhi = 0;
+      int prio_lo = 0, prio_hi = 0;
+      NBG_CUDA(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+      for (size_t q = 0; q < ng; q++) {
+        const bool hi = ng > 1 && 2.0 * chain_len(q) >= longest_all;
+        std::vector<cudaStream_t>& pool = hi ? ctx->hstreams : ctx->gstreams;
+        size_t& used = hi ? nhi : nlo;
+        while (pool.size() < used + 3) {
+          cudaStream_t s2;
+          NBG_CUDA(cudaStreamCreateWithPriority(&s2, cudaStreamNonBlocking, hi ? prio_hi : prio_lo));
+          pool.push_back(s2);
+        }
+        for (int r = 0; r < 3; r++) gstr[3 * q + r] = pool[used + r];
+        used += 3;
+      }
     }
     cudaEvent_t evs;
     if ((rc = ctx->sync_event(0, &evs))) return rc;
     NBG_CUDA(cudaEventRecord(evs, st));
-    for (size_t q = 0; q < 3 * ng; q++) NBG_CUDA(cudaStreamWaitEvent(ctx->gstreams[q], evs, 0));  // after the packing
+    for (size_t q = 0; q < 3 * ng; q++) NBG_CUDA(cudaStreamWaitEvent(gstr[q], evs, 0));  // after the packing
     for (long long c = 0; c < nchunks; c++) {
       for (size_t q = 0; q < ng; q++) {
         if (c * K >= gmaxsteps[q]) continue;
         const int par = (int)(c & 1);
         const GroupArgs& g = par ? ghalf[q] : gargs[q];
-        cudaStream_t sp = ctx->gstreams[3 * q], sw = ctx->gstreams[3 * q + 1], stt = ctx->gstreams[3 * q + 2];
+        cudaStream_t sp = gstr[3 * q], sw = gstr[3 * q + 1], stt = gstr[3 * q + 2];
         cudaEvent_t ev_orb, ev_done, ev_tr;
         if ((rc = ctx->sync_event(2 + 6 * q + par, &ev_orb)) || (rc = ctx->sync_event(4 + 6 * q + par, &ev_done)) ||
             (rc = ctx->sync_event(6 + 6 * q + par, &ev_tr)))
@@ -818,7 +845,7 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     for (size_t q = 0; q < 3 * ng; q++) {
       cudaEvent_t ej;
       if ((rc = ctx->sync_event(1, &ej))) return rc;
-      NBG_CUDA(cudaEventRecord(ej, ctx->gstreams[q]));
+      NBG_CUDA(cudaEventRecord(ej, gstr[q]));
       NBG_CUDA(cudaStreamWaitEvent(st, ej, 0));
     }
   }
@@ -1333,6 +1360,7 @@ int nbg_destroy(nbg_context* ctx) {
   // every stream of the context is idle before its buffers are freed
   cudaStreamSynchronize(ctx->stream);
   for (cudaStream_t s2 : ctx->gstreams) cudaStreamSynchronize(s2);
+  for (cudaStream_t s2 : ctx->hstreams) cudaStreamSynchronize(s2);
   for (auto& kv : ctx->pool)
     if (kv.second.p) cudaFree(kv.second.p);
   cudaEventDestroy(ctx->ev0);
@@ -1340,6 +1368,7 @@ int nbg_destroy(nbg_context* ctx) {
   for (auto e : ctx->prof_events) cudaEventDestroy(e);
   for (auto e : ctx->sync_events) cudaEventDestroy(e);
   for (cudaStream_t s2 : ctx->gstreams) cudaStreamDestroy(s2);
+  for (cudaStream_t s2 : ctx->hstreams) cudaStreamDestroy(s2);
   cudaStreamDestroy(ctx->stream);
   delete ctx->noalloc;
   delete ctx;
