@@ -9,6 +9,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <deque>
+#include <thread>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
@@ -803,9 +805,36 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
     if ((rc = ctx->sync_event(0, &evs))) return rc;
     NBG_CUDA(cudaEventRecord(evs, st));
     for (size_t q = 0; q < 3 * ng; q++) NBG_CUDA(cudaStreamWaitEvent(gstr[q], evs, 0));  // after the packing
-    for (long long c = 0; c < nchunks; c++) {
+    // Each group is enqueued at its own pace: at most kAhead of its chunks are
+    // queued on the GPU, and the host adds a group's next chunk once one of
+    // its queued chunks has completed (an event per chunk, polled).  Groups of
+    // short or cheap systems thus run ahead and finish, instead of being held
+    // to the slowest group's pace by a launch queue that the slowest group
+    // keeps full.
+    constexpr int kAhead = 4;
+    std::vector<long long> next_chunk(ng, 0), nch(ng);
+    std::vector<std::deque<long long>> queued(ng);
+    for (size_t q = 0; q < ng; q++) nch[q] = (gmaxsteps[q] + K - 1) / K;
+    auto chunk_event = [&](size_t q, long long c, cudaEvent_t* ev) {
+      return ctx->sync_event(8 + 6 * ng + (kAhead + 1) * q + (size_t)(c % (kAhead + 1)), ev);
+    };
+    size_t remaining = 0;
+    for (size_t q = 0; q < ng; q++) remaining += nch[q] > 0 ? 1 : 0;
+    while (remaining > 0) {
+      bool progressed = false;
       for (size_t q = 0; q < ng; q++) {
-        if (c * K >= gmaxsteps[q]) continue;
+        while (!queued[q].empty()) {
+          cudaEvent_t evq;
+          if ((rc = chunk_event(q, queued[q].front(), &evq))) return rc;
+          const cudaError_t e = cudaEventQuery(evq);
+          if (e == cudaErrorNotReady) break;
+          if (e != cudaSuccess) return set_error(NBG_ECUDA, "chunk failed: %s", cudaGetErrorString(e));
+          queued[q].pop_front();
+        }
+        if (next_chunk[q] >= nch[q] || (int)queued[q].size() >= kAhead) continue;
+        const long long c = next_chunk[q]++;
+        if (next_chunk[q] == nch[q]) remaining--;
+        progressed = true;
         const int par = (int)(c & 1);
         const GroupArgs& g = par ? ghalf[q] : gargs[q];
         cudaStream_t sp = gstr[3 * q], sw = gstr[3 * q + 1], stt = gstr[3 * q + 2];
@@ -838,7 +867,12 @@ int run_batch(nbg_context* ctx, int nsys, const nbg_system_desc* desc, const dou
         }
         if ((rc = copy_traj(q, g, c, sw))) return rc;
         NBG_CUDA(cudaEventRecord(ev_done, sw));
+        cudaEvent_t evq;
+        if ((rc = chunk_event(q, c, &evq))) return rc;
+        NBG_CUDA(cudaEventRecord(evq, sw));
+        queued[q].push_back(c);
       }
+      if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
     // join: everything after runs on st (an event recorded on a stream and
     // waited on at once may be re-recorded for the next stream)
