@@ -485,6 +485,15 @@ def latency_table(nbg, device, steps=(256, 768)):
             name = {0: "one_lane", 1: "team", 2: "wide"}[team]
             row[name] = (best[steps[1]] - best[steps[0]]) * 1e3 / (steps[1] - steps[0])
             row["call_fixed_ms_" + name] = best[steps[0]] * 1e3 - row[name] * steps[0]
+            # the kernels' summed device time per step in one more (longer) call, timed per launch
+            ctx.set_profiling(1)
+            s = nbg.State(ic)
+            tt = nbg.TransitTiming(steps[1] * h, ic)
+            nbg.Integrator(nbg.ahl21, h, 0.0, steps[1] * h)(s, tt, grad=True, ctx=ctx)
+            ctx.set_profiling(0)
+            tot, orb, tra, jac = ctx.last_timing()
+            row["kernels_ms_per_step_" + name] = {"orbit": orb / steps[1], "transit": tra / steps[1],
+                                                 "jacobian": jac / steps[1], "loop": tot / steps[1]}
             ctx.close()
         out[str(n)] = row
     return {"unit": "ms per grad step, one system per call (difference of two call lengths)", "steps": list(steps),

@@ -436,8 +436,9 @@ int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double
  * memory, operator and search blocks 32 KB} (nbg_set_producer_layout).  The
  * two trial times give the loop's fill and drain and its time per step with
  * the whole batch active.  For a batch of uneven length (its shortest system
- * under half its longest) two more trials run only its longest systems (at
- * most 32) for the chain's time per step, and the predicted time sums, step
+ * under half its longest) two more trials run only the systems with its
+ * longest chains (steps times 2N - 3, at most 32) for the chain's time per
+ * step, and the predicted time sums, step
  * by step, the time per step for the work still active: the power law
  * through the two measured ends (the whole batch; the chain set alone),
  * never below the chain's; for an even batch it extrapolates the two trials

@@ -1969,15 +1969,15 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
   }
   std::sort(dist.begin(), dist.end());
   const bool uneven = longest > 0 && (double)shortest < 0.5 * (double)longest;
-  // the chain set: the longest systems (at most 32), the rest shortened to zero steps
+  // the chain set: the systems with the longest chains (at most 32), the rest shortened to zero steps
   std::vector<nbg_system_desc> tc1(td1), tc2(td2);
   double wchain = wtot;
   if (uneven) {
     std::vector<int> ord(nsys);
     for (int s = 0; s < nsys; s++) ord[s] = s;
-    std::sort(ord.begin(), ord.end(), [&](int a, int b) {
-      return steps_of(desc[a].h, desc[a].tmax) > steps_of(desc[b].h, desc[b].tmax);
-    });
+    // longest chains first: steps times 2N - 3, the pair solves on the critical path of a team step
+    auto chain = [&](int q) { return (double)steps_of(desc[q].h, desc[q].tmax) * (2.0 * desc[q].n - 3.0); };
+    std::sort(ord.begin(), ord.end(), [&](int a, int b) { return chain(a) > chain(b); });
     const int nchain = std::min(32, std::max(1, nsys / 64));
     wchain = 0.0;
     for (int q = 0; q < nchain; q++) {
