@@ -62,10 +62,13 @@ def flops_per_system_step(n):
     Per column of jac_step and step: 2P pair updates of 132 flops (6 differences,
     a 6x6 product u = K D (66), the two mass-ratio scalings (12) and the Kahan
     sums of 12 rows (48)); the phi block 3N x 3N (18 N^2) with its Kahan sums
-    (12 N + 9 N); two kick folds (36 N); two drifts (30 N).  7N columns.
+    (12 N); two drifts (30 N).  The zero-addend folds of 6N, 3N and 6N rows
+    count one add per row (15 N): the warp tests s + e and runs the fold's
+    other two adds only when one would change a row, which after a
+    compensated add it almost never does.  7N columns.
     """
     P = n * (n - 1) // 2
-    per_col = 2 * P * 132 + 18 * n * n + 87 * n
+    per_col = 2 * P * 132 + 18 * n * n + 57 * n
     return per_col * 7 * n
 
 

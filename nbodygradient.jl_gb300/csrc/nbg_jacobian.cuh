@@ -28,6 +28,36 @@ __device__ __forceinline__ void fold(double& s, double& e) {
   s = t;
 }
 
+// Whether fold(s, e) changes s or e.  It leaves both bitwise unchanged exactly
+// when s + e rounds to s (same bits), s is finite (else s - s is NaN) and e is
+// not -0 ((s - s) + -0 is +0).  After a compensated add the pair is normally
+// in that state: the add leaves in e the rounding error of s, which s + e
+// rounds away.  The test costs one FP64 add against the fold's three; the
+// rest is integer work.
+__device__ __forceinline__ bool fold_changes(double s, double e) {
+  const unsigned long long sb = __double_as_longlong(s), eb = __double_as_longlong(e);
+  const unsigned long long tb = __double_as_longlong(s + e);
+  return tb != sb || ((sb >> 52) & 0x7ffull) == 0x7ffull || eb == 0x8000000000000000ull;
+}
+
+// fold() on rows 6 b + R0 .. 6 b + R0 + NR - 1 of every body b.  The warp
+// first tests its lanes' rows and runs the folds only if one of them would
+// change a row, so the result is the folds' result bitwise (each lane skips
+// only when no lane of its group, itself included, would change).
+template <int N, int BS, int R0, int NR>
+__device__ __forceinline__ void fold_rows(double* J, double* E) {
+  bool change = false;
+#pragma unroll 1
+  for (int b = 0; b < N; b++)
+#pragma unroll
+    for (int r = R0; r < R0 + NR; r++) change |= fold_changes(J[(6 * b + r) * BS], E[(6 * b + r) * BS]);
+  if (!__any_sync(__activemask(), change)) return;
+#pragma unroll 1
+  for (int b = 0; b < N; b++)
+#pragma unroll
+    for (int r = R0; r < R0 + NR; r++) fold(J[(6 * b + r) * BS], E[(6 * b + r) * BS]);
+}
+
 // P[vr] = (A J)[velocity row vr] for the compact operator at record offset
 // roff: one FMA chain over the position rows of J, with the exact no-op
 // terms (zero operator entries; mass rows of J, which are unit rows) reduced
@@ -74,23 +104,19 @@ __device__ __forceinline__ void pair_apply(double* J, double* E, int c, int i, i
 }
 
 // J <- J + A J on all non-mass rows: velocity rows take the product P,
-// position rows a zero addend.
+// position rows a zero addend.  Every row is summed on its own, so the
+// position rows' folds may run first.
 template <int N, int BS>
 __device__ __forceinline__ void add_velocity_rows(double* J, double* E, const double* P) {
-#pragma unroll 1
-  for (int b = 0; b < N; b++) {
-#pragma unroll
-    for (int k = 0; k < 3; k++) fold(J[(6 * b + k) * BS], E[(6 * b + k) * BS]);
-#pragma unroll
-    for (int k = 0; k < 3; k++) kahan(J[(6 * b + 3 + k) * BS], E[(6 * b + 3 + k) * BS], P[3 * b + k]);
-  }
-}
-template <int N, int BS>
-__device__ __forceinline__ void fold_all(double* J, double* E) {
+  fold_rows<N, BS, 0, 3>(J, E);
 #pragma unroll 1
   for (int b = 0; b < N; b++)
 #pragma unroll
-    for (int r = 0; r < 6; r++) fold(J[(6 * b + r) * BS], E[(6 * b + r) * BS]);
+    for (int k = 0; k < 3; k++) kahan(J[(6 * b + 3 + k) * BS], E[(6 * b + 3 + k) * BS], P[3 * b + k]);
+}
+template <int N, int BS>
+__device__ __forceinline__ void fold_all(double* J, double* E) {
+  fold_rows<N, BS, 0, 6>(J, E);
 }
 
 // drift_grad! on jac_step (ahl21.jl:318-331): x rows += h * v rows.
