@@ -82,24 +82,32 @@ __device__ __forceinline__ void op_product(const double* J, const Rec& rec, int 
 }
 
 // One Kepler pair block update (ahl21.jl:31-42 / :64-75) on this column.
+// The pair's record is loaded first, all of it, so that its loads go out
+// together ahead of this pair's stores to J and E (which a load through the
+// record pointer could alias): one trip to memory per pair.  A system alone
+// on the GPU waits out every such trip, at ten bodies 90 of them per step.
 template <int N, int BS>
 __device__ __forceinline__ void pair_apply(double* J, double* E, int c, int i, int j, const Rec& rec, int roff) {
-  double D[6];
+  double K[36];
 #pragma unroll
-  for (int l = 0; l < 6; l++) D[l] = J[(6 * i + l) * BS] - J[(6 * j + l) * BS];
+  for (int q = 0; q < 36; q++) K[q] = rec.get(roff + q);
   const double mi = rec.get(roff + PREC_MI), mj = rec.get(roff + PREC_MJ);
   // the mass column of body i or j (at most one of them is this column)
   // takes the pair's mass entries; every other column adds an exact zero
   const int mc = (c == 7 * i + 6) ? PREC_MC6 : (c == 7 * j + 6) ? PREC_MC13 : -1;
+  double C[12];
+#pragma unroll
+  for (int q = 0; q < 12; q++) C[q] = (mc >= 0) ? rec.get(roff + mc + q) : 0.0;
+  double D[6];
+#pragma unroll
+  for (int l = 0; l < 6; l++) D[l] = J[(6 * i + l) * BS] - J[(6 * j + l) * BS];
 #pragma unroll
   for (int r = 0; r < 6; r++) {
-    double u = rec.get(roff + r * 6) * D[0];
+    double u = K[r * 6] * D[0];
 #pragma unroll
-    for (int l = 1; l < 6; l++) u = fma(rec.get(roff + r * 6 + l), D[l], u);
-    const double ci = (mc >= 0) ? rec.get(roff + mc + r) : 0.0;
-    const double cj = (mc >= 0) ? rec.get(roff + mc + 6 + r) : 0.0;
-    kahan(J[(6 * i + r) * BS], E[(6 * i + r) * BS], fma(mj, u, ci));
-    kahan(J[(6 * j + r) * BS], E[(6 * j + r) * BS], fma(-mi, u, cj));
+    for (int l = 1; l < 6; l++) u = fma(K[r * 6 + l], D[l], u);
+    kahan(J[(6 * i + r) * BS], E[(6 * i + r) * BS], fma(mj, u, C[r]));
+    kahan(J[(6 * j + r) * BS], E[(6 * j + r) * BS], fma(-mi, u, C[6 + r]));
   }
 }
 
