@@ -442,7 +442,11 @@ int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double
  * by step, the time per step for the work still active: the power law
  * through the two measured ends (the whole batch; the chain set alone),
  * never below the chain's; for an even batch it extrapolates the two trials
- * to the longest system.  trial_ms reports the trials' times.  The fastest candidate is kept on the
+ * to the longest system.  trial_ms reports the trials' times.  Before the
+ * timed trials, untimed runs launch every kernel form the candidates use
+ * (one-lane and team producers; for an uneven batch also the chain set's wide
+ * form and team searches), so that no trial carries a kernel's first-launch
+ * module loading.  The fastest candidate is kept on the
  * context (as nbg_set_tuning / nbg_set_orbit_team / nbg_set_orbit_lanes
  * would).  Arrays as for nbg_batch_integrate_transits_device.  report (may
  * be NULL) receives up to report_len candidates; *nreport (may be NULL)

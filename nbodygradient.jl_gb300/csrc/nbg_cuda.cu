@@ -2034,8 +2034,33 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
   int best = -1, nrep = 0;
   double best_ms = 1e300;
   std::vector<double> cand_ms;
-  for (size_t q = 0; q <= cands.size(); q++) {
-    const Cand& cd = cands[q == 0 ? 0 : q - 1];  // the first candidate runs twice: the first run allocates
+  rc = NBG_OK;
+  // Untimed warm-up.  The first run of a batch allocates the context's
+  // buffers (grow-only, so at the longest chunk of the candidates), and with
+  // lazy module loading (the CUDA default) the first launch of each kernel
+  // loads it.  Every kernel a candidate can launch runs once here: the
+  // one-lane producer, the team producer and, for an uneven batch, the chain
+  // set, whose groups take the wide form and the team searches.  Otherwise the
+  // first trial to allocate or to use a kernel would carry that cost, and the
+  // difference of two trial lengths would understate a step's time.
+  int wchunk = 0;
+  for (const Cand& cd : cands) wchunk = std::max(wchunk, cd.chunk);
+  for (int wteam : {0, 3}) {
+    if (wteam && !any_team) continue;
+    ctx->chunk_steps = wchunk;
+    ctx->orbit_team = wteam;
+    ctx->orbit_spw = cands[0].spw;
+    ctx->prod_warps = cands[0].pw;
+    ctx->prod_smem_kb = cands[0].smem;
+    ctx->guard_smem_kb = cands[0].guard;
+    for (int r = 0; r < (uneven ? 2 : 1) && !rc; r++) {
+      if ((rc = reset())) break;
+      rc = run_batch(ctx, nsys, r == 0 ? td1.data() : tc1.data(), th.data(), ph.data(), c_t, c_x, c_v, m, c_xe, c_ve,
+                     c_J, c_E, c_dq, jac_init, c_tt, c_dq0, c_del, c_cnt, nullptr);
+    }
+  }
+  for (size_t q = 1; q <= cands.size() && !rc; q++) {
+    const Cand& cd = cands[q - 1];
     ctx->chunk_steps = cd.chunk;
     ctx->orbit_team = cd.team ? 3 : 0;  // a team, wide in latency-bound chunks
     ctx->orbit_spw = cd.spw;
@@ -2043,7 +2068,7 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
     ctx->prod_smem_kb = cd.smem;
     ctx->guard_smem_kb = cd.guard;
     double tms[4] = {0.0, 0.0, 0.0, 0.0};
-    const int ntrials = (uneven && q > 0) ? 4 : 2;
+    const int ntrials = uneven ? 4 : 2;
     for (int r = 0; r < ntrials && !rc; r++) {
       if ((rc = reset())) break;
       const nbg_system_desc* dd = r == 0 ? td1.data() : r == 1 ? td2.data() : r == 2 ? tc1.data() : tc2.data();
@@ -2052,7 +2077,6 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
       tms[r] = ctx->last_total_ms;
     }
     if (rc) break;
-    if (q == 0) continue;
     const double T1 = std::min<long long>(longest, trial_steps), T2 = std::min<long long>(longest, 2LL * trial_steps);
     const double slope = (T2 > T1) ? std::max(0.0, (tms[1] - tms[0]) / (T2 - T1)) : 0.0;
     double ms = (T2 > T1) ? tms[0] + slope * ((double)longest - T1) : tms[1];
