@@ -438,10 +438,9 @@ int nbg_last_timing(nbg_context* ctx, double* total_ms, double* orbit_ms, double
  * the whole batch active.  For a batch of uneven length (its shortest system
  * under half its longest) two more trials run only the systems with its
  * longest chains (steps times 2N - 3, at most 32) for the chain's time per
- * step, and the predicted time sums, step
- * by step, the time per step for the work still active: the power law
- * through the two measured ends (the whole batch; the chain set alone),
- * never below the chain's; for an even batch it extrapolates the two trials
+ * step, and the predicted time sums, step by step, the whole batch's time
+ * per step scaled by the Jacobian work still active, never below the
+ * chain's; for an even batch it extrapolates the two trials
  * to the longest system.  trial_ms reports the trials' times.  Before the
  * timed trials, untimed runs launch every kernel form the candidates use
  * (one-lane and team producers; for an uneven batch also the chain set's wide

@@ -1971,7 +1971,6 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
   const bool uneven = longest > 0 && (double)shortest < 0.5 * (double)longest;
   // the chain set: the systems with the longest chains (at most 32), the rest shortened to zero steps
   std::vector<nbg_system_desc> tc1(td1), tc2(td2);
-  double wchain = wtot;
   if (uneven) {
     std::vector<int> ord(nsys);
     for (int s = 0; s < nsys; s++) ord[s] = s;
@@ -1979,11 +1978,6 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
     auto chain = [&](int q) { return (double)steps_of(desc[q].h, desc[q].tmax) * (2.0 * desc[q].n - 3.0); };
     std::sort(ord.begin(), ord.end(), [&](int a, int b) { return chain(a) > chain(b); });
     const int nchain = std::min(32, std::max(1, nsys / 64));
-    wchain = 0.0;
-    for (int q = 0; q < nchain; q++) {
-      const int n = desc[ord[q]].n, P = n * (n - 1) / 2;
-      wchain += 7.0 * n * (264.0 * P + 18.0 * n * n + 87.0 * n);
-    }
     for (int q = nchain; q < nsys; q++) {
       tc1[ord[q]].tmax = 0.0;
       tc2[ord[q]].tmax = 0.0;
@@ -2083,13 +2077,9 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
     if (uneven && T2 > T1) {
       const double fill = std::max(0.0, tms[0] - slope * T1);
       const double chain = std::max(0.0, (tms[3] - tms[2]) / (T2 - T1));
-      // The time per step falls from `slope` with the whole batch active to
-      // `chain` with only the chain set's work (fraction fc) left.  Fewer
-      // systems use the GPU less well, so it does not fall in proportion to
-      // the work: between the two measured ends it follows the power law
-      // through both, slope * f^a with a = log(slope / chain) / log(1 / fc).
-      const double fc = std::min(0.999, std::max(1e-9, wchain / wtot));
-      const double a = (slope > chain && chain > 0.0) ? std::log(slope / chain) / std::log(1.0 / fc) : 1.0;
+      // The time per step falls from `slope` with the whole batch active in
+      // proportion to the Jacobian work still active (fraction f), but never
+      // below `chain`, the step of the longest chains running alone.
       // walk the steps: between consecutive system lengths the active work is constant
       double model = fill, active = wtot;
       long long k = 0;
@@ -2098,7 +2088,7 @@ int nbg_autotune_device(nbg_context* ctx, int nsys, const nbg_system_desc* desc,
         while (at < dist.size() && dist[at].first <= k) active -= dist[at++].second;
         const long long next = at < dist.size() ? dist[at].first : longest;
         const double f = std::max(0.0, active / wtot);
-        model += (double)(next - k) * std::max(slope * std::pow(f, a), chain);
+        model += (double)(next - k) * std::max(slope * f, chain);
         k = next;
       }
       ms = model;
